@@ -1,0 +1,385 @@
+"""Benchmark of the GB300 PBF step (one JSON line on stdout).
+
+Workload (default): the 1,048,576-particle dam break - a 128x64x128 jittered
+lattice (spacing 0.01, jitter +-0.0005 from mt19937_64(0xC0FFEE)) in the
+[0,2]x[0,1]x[0,2] box, h = 2.5r, 2 solver iterations, hashed grid.  A "step"
+is one full simulation step of all particles.  W warm-up steps from the
+seeded lattice, then K timed steps; L2 is flushed (256 MiB write) before every
+timed step and each step is timed with CUDA events on the simulator's stream.
+
+  value      particle-steps/s, state resident in HBM
+  e2e        the same through pbf_step_host: pinned host pos/vel copied in,
+             one step, copied back, every step (wall clock)
+  roofline   dominant kernel of the step (from a live per-phase profile):
+             algorithmic bytes per launch / its CUDA-event time, vs the
+             measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (OpenMP, all host threads) on a bounded
+             sample of the same workload (rank 0, N = 1)
+
+--impl reference times the reference arm: the reference has no CPU PBF path
+(sim/kernel_fallback.cpp is a vector add), so its CPU implementation is the
+restatement in oracle/, run on all host threads.
+
+Multi-GPU: the path does not shard (a single scene needs halo exchanges), so
+--gpus N runs N independent replicas ("scaling": "weak"); value = all ranks'
+particle-steps / the slowest rank's timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cuda-pbf-fluid-sim_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: box, lattice, solver iters, grid, second block (lattice, origin seed)
+    "c1": dict(box=(1.0, 1.0, 1.0), lattice=(32, 32, 32), iters=2, hashed=True,
+               workload="dam_break_32k_2iter_hashed (32x32x32 lattice, [0,1]^3 box)"),
+    "c2": dict(box=(2.0, 1.0, 2.0), lattice=(128, 64, 128), iters=2, hashed=True,
+               workload="dam_break_1M_2iter_hashed (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
+    "c2_dense": dict(box=(2.0, 1.0, 2.0), lattice=(128, 64, 128), iters=2, hashed=False,
+                     workload="dam_break_1M_2iter_dense (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
+}
+
+METRIC = "particle-steps/s @1M"
+UNIT = "particle-steps/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def key_bits(num_cells: int) -> int:
+    return max(1, int(num_cells - 1).bit_length())
+
+
+def alg_bytes_per_particle(phase: str, n: int, num_cells: int, hashed: bool, iters: int) -> float:
+    """Compulsory bytes per particle of one launch of each phase (neighbour
+    gathers counted once; float4 state, u32 keys/ids)."""
+    passes = (key_bits(num_cells) + 7) // 8
+    table = 4.0 * (num_cells + 1) / max(n, 1)
+    if phase == "predict_keys":
+        return 16 + 16 + 4  # R pos, vel; W key
+    if phase == "sort":
+        return 4 + 4 + 8 + 16 * (passes - 1)  # histogram read, first pass R key W pair, then R/W pairs
+    if phase == "gather_tables":
+        return 4 + 16 + 16 + 16 + 16 + 4 + table + (12 if hashed else 0)
+    if phase.startswith("lambda"):
+        return 16 + 4 + 4  # R pred, key; W lambda (table reads shared by a cell)
+    if phase.startswith("delta"):
+        last = phase == "delta_%d" % iters
+        return 16 + 4 + 4 + 16 + (32 if last else 0)  # R pred, lambda, key; W pred (+ R pos_s, W vel)
+    if phase == "commit":
+        return 16 + 16 + 4 + 4 + 16 + 16  # R pred, vel_s, key, perm; W pos, vel
+    return 0.0
+
+
+def step_alg_bytes(num_cells: int, iters: int) -> float:
+    """Whole-step compulsory bytes: 202 + 16 P + 60 iters per particle."""
+    passes = (key_bits(num_cells) + 7) // 8
+    return 202 + 16 * passes + 60 * iters
+
+
+class ClockSampler:
+    FIELDS = ("index,pci.bus_id,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, bus_id: str | None):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 10:
+                continue
+            rows.append(parts)
+        os.unlink(self.path)
+        if bus_id:
+            mine = [r for r in rows if r[1].lower().endswith(bus_id.lower()[-12:])]
+            rows = mine or rows
+        if not rows:
+            return None
+        sm = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, col in (("hw_slowdown", 6), ("hw_thermal_slowdown", 7), ("sw_thermal_slowdown", 8),
+                              ("sw_power_cap", 9)):
+                if r[col].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("PBF_BENCH_BACKEND", "") != "gloo" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def aggregate(local_seconds: float, local_units: float, world: int):
+    """Max of the timed region over ranks and sum of processed units."""
+    if world <= 1:
+        return local_seconds, local_units
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([local_seconds], dtype=torch.float64, device=dev)
+    u = torch.tensor([local_units], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def scene(lib, cfg):
+    import pbfx
+
+    nx, ny, nz = cfg["lattice"]
+    n = nx * ny * nz
+    p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
+    pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
+    return p, pos, np.zeros_like(pos)
+
+
+def cpu_rate(orc, p, hashed, pos, vel, budget_s: float, max_steps: int):
+    """Oracle steps from (pos, vel) until the budget is used; returns
+    (particle-steps/s, steps, seconds)."""
+    import pbfx
+
+    pos, vel = pos.copy(), vel.copy()
+    n = pos.shape[0]
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        pbfx.oracle_step(orc, p, hashed, pos, vel, trace=False)
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return n * steps / dt, steps, dt
+
+
+def run_reference(args, cfg, world, rank):
+    if rank != 0:
+        return 0
+    import __graft_entry__ as g
+    import pbfx
+
+    g.build_library()
+    g.build_oracle()
+    lib, orc = pbfx.load(), pbfx.load_oracle()
+    p, pos, vel = scene(lib, cfg)
+    n = pos.shape[0]
+    cores = orc.oracle_num_threads()
+    for _ in range(args.warmup):
+        pbfx.oracle_step(orc, p, cfg["hashed"], pos, vel, trace=False)
+    rate, steps, secs = cpu_rate(orc, p, cfg["hashed"], pos, vel, args.ref_budget, args.steps)
+    sample = ("%d of the %d requested steps of the %d-particle workload after %d warm-up steps "
+              "(time budget %.0f s)" % (steps, args.steps, n, args.warmup, args.ref_budget))
+    line = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+        "config": {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"],
+                   "grid": "hashed" if cfg["hashed"] else "dense", "implementation": "CPU restatement of the "
+                   "reference kernels (oracle/pbf_oracle.cpp), OpenMP over particles; the reference has no CPU "
+                   "PBF path"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, cfg, world, rank, local):
+    import torch
+
+    import __graft_entry__ as g
+    import pbfx
+
+    if rank == 0 or world == 1:
+        g.build_library()
+        g.build_oracle()
+    barrier(world)
+    torch.cuda.set_device(local)
+    lib = pbfx.load()
+    p, pos, vel = scene(lib, cfg)
+    n = pos.shape[0]
+    nc = pbfx.num_cells(p)
+    hashed = cfg["hashed"]
+    hbm_peak, peak_kind = peaks()
+
+    sim = pbfx.Sim(lib, p, hashed=hashed)
+    sim.upload(pos, vel)
+    stream = torch.cuda.ExternalStream(sim.stream_ptr())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    pp = C.byref(p)
+
+    for _ in range(args.warmup):
+        pbfx.check(lib.pbf_step(sim.h, pp))
+    pbfx.check(lib.pbf_synchronize(sim.h))
+    snap_pos, snap_vel = sim.download()  # state at the start of the timed region
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush, outside the timed window
+            ev[k][0].record(stream)
+            lib.pbf_step(sim.h, pp)
+            ev[k][1].record(stream)
+    pbfx.check(lib.pbf_synchronize(sim.h))
+    torch.cuda.synchronize()
+    barrier(world)
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id  # type: ignore[attr-defined]
+    except Exception:
+        bus = None
+    clk = clocks.stop(bus)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    local_s = sum(step_ms) / 1e3
+    total_s, units = aggregate(local_s, float(n) * args.steps, world)
+    value = units / total_s
+
+    # Live per-phase profile (after the timed region): dominant kernel.
+    prof = {}
+    for _ in range(args.profile_steps):
+        for name, ms in sim.profile_step():
+            prof.setdefault(name, []).append(ms)
+    avg = {k: sum(v) / len(v) for k, v in prof.items()}
+    total_phase = sum(avg.values())
+    dom = max(avg, key=avg.get)
+    dom_bytes = alg_bytes_per_particle(dom, n, nc, hashed, cfg["iters"]) * n
+    achieved = dom_bytes / (avg[dom] * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_c2.json")
+    if cfg is CONFIGS["c2"] and os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(dom.split("_")[0] if dom[-1].isdigit() else dom)
+
+    # End to end through host buffers.
+    e2e_steps = min(args.steps, args.e2e_steps)
+    hp = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    hv = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    pbfx.check(lib.pbf_download_state(sim.h, C.c_void_p(hp.data_ptr()), C.c_void_p(hv.data_ptr())))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        pbfx.check(lib.pbf_step_host(sim.h, pp, C.c_void_p(hp.data_ptr()), C.c_void_p(hv.data_ptr())))
+    e2e_s = time.perf_counter() - t0
+    e2e_total, e2e_units = aggregate(e2e_s, float(n) * e2e_steps, world)
+    launches = sim.launches_per_step() * args.steps
+    sim.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded jittered lattice, mt19937_64 0xC0FFEE)",
+        "config": {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"], "cells": nc,
+                   "grid": "hashed" if hashed else "dense", "parallelism": "replicas" if world > 1 else "single",
+                   "timed_steps": "steps %d..%d of the run from the seeded lattice" % (args.warmup,
+                                                                                     args.warmup + args.steps - 1),
+                   "l2": "flushed before every timed step (256 MiB write, untimed)"},
+        "e2e": {"value": e2e_units / e2e_total, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                "steps": e2e_steps, "api": "pbf_step_host (pinned host pos/vel in, one step, pos/vel out)"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes_per_launch": dom_bytes, "ms_per_launch": avg[dom],
+                     "share_of_step": avg[dom] / total_phase},
+        "step_roofline": {"alg_bytes_per_particle_step": step_alg_bytes(nc, cfg["iters"]),
+                          "achieved": value * step_alg_bytes(nc, cfg["iters"]) / 1e9, "peak": hbm_peak,
+                          "unit": "GB/s",
+                          "frac": value * step_alg_bytes(nc, cfg["iters"]) / 1e9 / hbm_peak},
+        "phase_ms": {k: round(v, 5) for k, v in avg.items()},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        orc = pbfx.load_oracle()
+        rate, steps, secs = cpu_rate(orc, p, hashed, snap_pos, snap_vel, args.cpu_budget, 1 << 30)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": orc.oracle_num_threads(), "kind": "port",
+                                "sample": "oracle FP32 steps %d..%d of the same run (%d particles), %.1f s" % (
+                                    args.warmup, args.warmup + steps - 1, n, secs)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    world, rank, local = dist_setup()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        return run_reference(args, cfg, world, rank)
+    return run_ours(args, cfg, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

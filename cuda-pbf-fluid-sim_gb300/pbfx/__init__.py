@@ -1,0 +1,346 @@
+"""ctypes binding of libpbf_gb300 (include/pbf/pbf.h) and of the CPU oracle.
+
+Host-side helper for tests, smoke() and bench.py: it only marshals arguments to
+the C ABI.  The library is loaded from this package's lib/ directory; loading
+fails loudly when it has not been built (there is no fallback path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ROOT = os.path.dirname(PKG_DIR)
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libpbf_gb300.so")
+ORACLE_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+
+PBF_OK = 0
+PBF_ERR_INVALID = 1
+PBF_ERR_CUDA = 2
+PBF_ERR_OOM = 3
+PBF_ERR_TIMEOUT = 4
+PBF_GRID_DENSE = 0
+PBF_GRID_HASHED = 1
+
+DBG_KEYS_SORTED = 0
+DBG_PERM = 1
+DBG_CELL_START = 2
+DBG_CELL_END = 3
+DBG_UNIQUE_KEYS = 4
+DBG_OFFSETS = 5
+DBG_COMPACT_COUNT = 6
+DBG_LAMBDA = 7
+DBG_NUM_CELLS = 8
+
+
+class Float3(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+
+class Int3(C.Structure):
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int)]
+
+
+class KernelCoeffs(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("h", "inv_h", "h2", "poly6", "spiky", "visc")]
+
+
+class GridBounds(C.Structure):
+    _fields_ = [("mins", Float3), ("maxs", Float3), ("cellSize", C.c_float), ("dim", Int3)]
+
+
+_TUNING = [
+    ("scorr_enable", C.c_int), ("scorr_k", C.c_float), ("scorr_n", C.c_float), ("scorr_dq_h", C.c_float),
+    ("wq_min", C.c_float), ("scorr_min", C.c_float), ("grad_r_eps", C.c_float), ("lambda_denom_eps", C.c_float),
+    ("compliance", C.c_float), ("xpbd_enable", C.c_int), ("enable_lambda_clamp", C.c_int),
+    ("lambda_max_abs", C.c_float), ("enable_disp_clamp", C.c_int), ("disp_clamp_max_h", C.c_float),
+    ("enable_relax", C.c_int), ("relax_omega", C.c_float), ("xsph_gate_enable", C.c_int), ("xsph_n_min", C.c_int),
+    ("xsph_n_max", C.c_int), ("lambda_warm_start_enable", C.c_int), ("lambda_warm_start_decay", C.c_float),
+    ("semi_implicit_integration_enable", C.c_int),
+]
+
+
+class Tuning(C.Structure):
+    _fields_ = _TUNING
+
+
+class SimParams(C.Structure):
+    _fields_ = [
+        ("numParticles", C.c_uint32), ("maxParticles", C.c_uint32), ("gravity", Float3), ("dt", C.c_float),
+        ("cfl", C.c_float), ("restDensity", C.c_float), ("solverIters", C.c_int), ("maxNeighbors", C.c_int),
+        ("sortEveryN", C.c_int), ("boundaryRestitution", C.c_float), ("particleMass", C.c_float), ("pbf", Tuning),
+        ("xsph_c", C.c_float), ("kernel", KernelCoeffs), ("grid", GridBounds), ("ghostParticleCount", C.c_uint32),
+    ]
+
+
+class DeviceParams(C.Structure):
+    _fields_ = [
+        ("kernel", KernelCoeffs), ("grid", GridBounds), ("gravity", Float3), ("restDensity", C.c_float),
+        ("dt", C.c_float), ("inv_dt", C.c_float), ("boundaryRestitution", C.c_float), ("maxNeighbors", C.c_int),
+        ("particleMass", C.c_float), ("pbf", Tuning), ("xsph_c", C.c_float),
+    ]
+
+
+class OracleTrace(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "keys", "keys_sorted", "perm", "cell_start", "cell_end", "unique_keys", "offsets", "compact_count",
+        "lambda_", "pred_solved", "vel_pre_xsph")]
+
+
+class OracleTable(C.Structure):
+    _fields_ = [("start", C.c_void_p), ("end", C.c_void_p), ("unique_keys", C.c_void_p), ("offsets", C.c_void_p),
+                ("count", C.c_uint32)]
+
+
+def ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+_VP, _U32, _I, _F, _SZ = C.c_void_p, C.c_uint32, C.c_int, C.c_float, C.c_size_t
+
+_SIGS = {
+    "pbf_status_string": ([_I], C.c_char_p),
+    "pbf_version": ([], _I),
+    "pbf_abi_sizes": ([C.POINTER(C.c_uint32 * 5)], None),
+    "pbf_default_tuning": ([C.POINTER(Tuning)], None),
+    "pbf_make_kernel_coeffs": ([_F, C.POINTER(KernelCoeffs)], None),
+    "pbf_make_device_params": ([C.POINTER(SimParams), C.POINTER(DeviceParams)], None),
+    "pbf_compute_dims": ([C.POINTER(GridBounds), C.POINTER(C.c_int32 * 3)], None),
+    "pbf_dam_break_params": ([_F, _F, _F, _I, _U32, C.POINTER(SimParams)], _I),
+    "pbf_seed_lattice": ([_VP, _U32, _U32, _U32, _F, _F, _F, _F, _F, C.c_uint64, C.POINTER(GridBounds)], _I),
+    "pbf_launch_integrate_pred": ([_VP, _VP, _VP, Float3, _F, _U32, _VP], _I),
+    "pbf_launch_boundary": ([_VP, _VP, C.POINTER(GridBounds), _F, _U32, _VP], _I),
+    "pbf_launch_velocity": ([_VP, _VP, _VP, _F, _U32, _VP], _I),
+    "pbf_launch_hash_keys": ([_VP, _VP, _VP, C.POINTER(GridBounds), _U32, _VP], _I),
+    "pbf_sort_pairs_query": ([C.POINTER(_SZ), _U32], _I),
+    "pbf_launch_sort_pairs": ([_VP, _SZ, _VP, _VP, _VP, _VP, _U32, _VP], _I),
+    "pbf_launch_sort_pairs_bits": ([_VP, _SZ, _VP, _VP, _VP, _VP, _U32, _I, _VP], _I),
+    "pbf_launch_cell_ranges": ([_VP, _VP, _VP, _U32, _U32, _VP], _I),
+    "pbf_cell_compact_scratch_query": ([C.POINTER(_SZ), _U32], _I),
+    "pbf_launch_cell_ranges_compact": ([_VP, _SZ, _VP, _VP, _VP, _VP, _U32, _VP], _I),
+    "pbf_launch_lambda": ([_VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
+    "pbf_launch_lambda_compact": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
+    "pbf_launch_delta_apply": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
+    "pbf_launch_delta_apply_compact": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP],
+                                       _I),
+    "pbf_launch_xsph": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
+    "pbf_launch_xsph_compact": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
+    "pbf_create": ([C.POINTER(SimParams), _I, C.POINTER(_VP)], _I),
+    "pbf_destroy": ([_VP], _I),
+    "pbf_stream": ([_VP], _VP),
+    "pbf_device_state": ([_VP, C.POINTER(_VP), C.POINTER(_VP)], _I),
+    "pbf_upload_state": ([_VP, _VP, _VP], _I),
+    "pbf_download_state": ([_VP, _VP, _VP], _I),
+    "pbf_step": ([_VP, C.POINTER(SimParams)], _I),
+    "pbf_step_n": ([_VP, C.POINTER(SimParams), _I], _I),
+    "pbf_step_host": ([_VP, C.POINTER(SimParams), _VP, _VP], _I),
+    "pbf_synchronize": ([_VP], _I),
+    "pbf_density_stats": ([_VP, C.POINTER(C.c_double * 4)], _I),
+    "pbf_debug_fetch": ([_VP, _I, _VP, _SZ], _I),
+    "pbf_selftest_bounded_wait": ([_U32, _VP], _I),
+    "pbf_profile_step": ([_VP, C.POINTER(SimParams), C.POINTER(C.c_float), C.POINTER(C.c_char_p), _I,
+                          C.POINTER(_I)], _I),
+    "pbf_launches_per_step": ([_VP], _I),
+}
+
+_ORACLE_SIGS = {
+    "oracle_num_threads": ([], _I),
+    "oracle_set_num_threads": ([_I], None),
+    "oracle_integrate_pred": ([_VP, _VP, _VP, Float3, _F, _U32], None),
+    "oracle_boundary": ([_VP, _VP, C.POINTER(GridBounds), _F, _U32], None),
+    "oracle_velocity": ([_VP, _VP, _VP, _F, _U32], None),
+    "oracle_hash_keys": ([_VP, _VP, _VP, C.POINTER(GridBounds), _U32], None),
+    "oracle_sort_pairs": ([_VP, _VP, _VP, _VP, _U32], None),
+    "oracle_cell_ranges": ([_VP, _VP, _VP, _U32, _U32], None),
+    "oracle_cell_ranges_compact": ([_VP, _VP, _VP, _VP, _U32], None),
+    "oracle_lambda": ([_VP, _VP, _VP, _VP, C.POINTER(OracleTable), C.POINTER(DeviceParams), _U32], None),
+    "oracle_delta_apply": ([_VP, _VP, _VP, _VP, _VP, C.POINTER(OracleTable), C.POINTER(DeviceParams), _U32], None),
+    "oracle_xsph": ([_VP, _VP, _VP, _VP, _VP, C.POINTER(OracleTable), C.POINTER(DeviceParams), _U32], None),
+    "oracle_step_f32": ([C.POINTER(SimParams), _I, _VP, _VP, _U32, C.POINTER(OracleTrace)], _I),
+    "oracle_step_f64": ([C.POINTER(SimParams), _I, _VP, _VP, _U32], _I),
+    "oracle_density_stats_f32pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
+    "oracle_density_stats_f64pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
+}
+
+
+def _bind(lib, sigs):
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+_lib = None
+_oracle = None
+
+
+def load(path: str = LIB_PATH):
+    """The CUDA library.  Raises if it is missing (no CPU fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("libpbf_gb300.so not built: run __graft_entry__.build()")
+        _lib = _bind(C.CDLL(path), _SIGS)
+    return _lib
+
+
+def load_oracle(path: str = ORACLE_PATH):
+    """The CPU oracle (test infrastructure only)."""
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(path):
+            raise RuntimeError("oracle not built: run __graft_entry__.build()")
+        _oracle = _bind(C.CDLL(path), _ORACLE_SIGS)
+    return _oracle
+
+
+def check(status: int, what: str = "call"):
+    if status != PBF_OK:
+        msg = load().pbf_status_string(status).decode()
+        raise RuntimeError("%s failed: %d (%s)" % (what, status, msg))
+
+
+def dam_break_params(box, iters: int = 2, num_particles: int = 0) -> SimParams:
+    p = SimParams()
+    check(load().pbf_dam_break_params(box[0], box[1], box[2], iters, num_particles, C.byref(p)), "dam_break_params")
+    return p
+
+
+def device_params(p: SimParams) -> DeviceParams:
+    d = DeviceParams()
+    load().pbf_make_device_params(C.byref(p), C.byref(d))
+    return d
+
+
+def num_cells(p: SimParams) -> int:
+    return int(p.grid.dim.x) * int(p.grid.dim.y) * int(p.grid.dim.z)
+
+
+def seed_lattice(lib, nx, ny, nz, origin, spacing, jitter, seed, params: SimParams) -> np.ndarray:
+    out = np.zeros((nx * ny * nz, 4), dtype=np.float32)
+    check(lib.pbf_seed_lattice(ptr(out), nx, ny, nz, origin[0], origin[1], origin[2], spacing, jitter, seed,
+                               C.byref(params.grid)), "seed_lattice")
+    return out
+
+
+def rel_err(a, b, floor_frac: float = 1e-2) -> float:
+    """max_i |a_i - b_i| / max(|b_i|, floor_frac * max_j |b_j|)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if b.size == 0:
+        return 0.0
+    scale = np.max(np.abs(b))
+    floor = floor_frac * scale if scale > 0 else 1e-30
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+def assert_close(a, b, tol: float, what: str, floor_frac: float = 1e-2):
+    e = rel_err(a, b, floor_frac)
+    if not e <= tol:
+        raise AssertionError("%s: relative error %.3e > %.1e" % (what, e, tol))
+
+
+class Sim:
+    """Owning wrapper of a pbf_sim handle."""
+
+    def __init__(self, lib, params: SimParams, hashed: bool = True):
+        self.lib = lib
+        self.params = params
+        self.h = C.c_void_p()
+        check(lib.pbf_create(C.byref(params), PBF_GRID_HASHED if hashed else PBF_GRID_DENSE, C.byref(self.h)),
+              "pbf_create")
+        self.n = int(params.numParticles)
+
+    def close(self):
+        if self.h:
+            self.lib.pbf_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, pos: np.ndarray, vel: np.ndarray):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        assert pos.shape == (self.n, 4) and vel.shape == (self.n, 4)
+        check(self.lib.pbf_upload_state(self.h, ptr(pos), ptr(vel)), "upload")
+
+    def download(self):
+        pos = np.zeros((self.n, 4), np.float32)
+        vel = np.zeros((self.n, 4), np.float32)
+        check(self.lib.pbf_download_state(self.h, ptr(pos), ptr(vel)), "download")
+        return pos, vel
+
+    def step(self, n: int = 1, params: SimParams | None = None):
+        check(self.lib.pbf_step_n(self.h, C.byref(params) if params is not None else None, n), "step")
+        check(self.lib.pbf_synchronize(self.h), "synchronize")
+
+    def fetch(self, item: int):
+        if item in (DBG_CELL_START, DBG_CELL_END):
+            cnt = num_cells(self.params)
+        elif item == DBG_OFFSETS:
+            cnt = self.n + 1
+        elif item in (DBG_COMPACT_COUNT, DBG_NUM_CELLS):
+            cnt = 1
+        else:
+            cnt = self.n
+        dt = np.float32 if item == DBG_LAMBDA else np.uint32
+        out = np.zeros(cnt, dtype=dt)
+        check(self.lib.pbf_debug_fetch(self.h, item, ptr(out), out.nbytes), "debug_fetch")
+        return out
+
+    def profile_step(self, params: SimParams | None = None):
+        ms = (C.c_float * 32)()
+        names = (C.c_char_p * 32)()
+        cnt = C.c_int()
+        check(self.lib.pbf_profile_step(self.h, C.byref(params) if params is not None else None, ms, names, 32,
+                                        C.byref(cnt)), "profile_step")
+        return [(names[k].decode(), float(ms[k])) for k in range(cnt.value)]
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.pbf_launches_per_step(self.h))
+
+    def stream_ptr(self) -> int:
+        return int(self.lib.pbf_stream(self.h) or 0)
+
+    def density_stats(self):
+        out = (C.c_double * 4)()
+        check(self.lib.pbf_density_stats(self.h, C.byref(out)), "density_stats")
+        return list(out)
+
+
+def oracle_step(orc, params: SimParams, hashed: bool, pos: np.ndarray, vel: np.ndarray, trace: bool = True):
+    """One FP32 oracle step in place; returns the trace arrays."""
+    n = int(pos.shape[0])
+    nc = num_cells(params)
+    tr = {}
+    t = OracleTrace()
+    if trace:
+        tr = {
+            "keys": np.zeros(n, np.uint32), "keys_sorted": np.zeros(n, np.uint32), "perm": np.zeros(n, np.uint32),
+            "lambda": np.zeros(n, np.float32), "pred_solved": np.zeros((n, 4), np.float32),
+            "vel_pre_xsph": np.zeros((n, 4), np.float32),
+        }
+        if hashed:
+            tr["unique_keys"] = np.zeros(max(n, 1), np.uint32)
+            tr["offsets"] = np.zeros(n + 1, np.uint32)
+            tr["compact_count"] = np.zeros(1, np.uint32)
+        else:
+            tr["cell_start"] = np.zeros(nc, np.uint32)
+            tr["cell_end"] = np.zeros(nc, np.uint32)
+        for k, v in tr.items():
+            setattr(t, "lambda_" if k == "lambda" else k, v.ctypes.data)
+    rc = orc.oracle_step_f32(C.byref(params), 1 if hashed else 0, ptr(pos), ptr(vel), n, C.byref(t) if trace else None)
+    if rc != 0:
+        raise RuntimeError("oracle_step_f32 failed")
+    if trace and hashed:
+        m = int(tr["compact_count"][0])
+        tr["unique_keys"] = tr["unique_keys"][:m]
+        tr["offsets"] = tr["offsets"][: m + 1]
+    return tr

@@ -1,0 +1,81 @@
+// device_buffers.h - device buffers of one simulation (GB300 layout).
+//
+// Keeps the reference's buffer names (sim/device_buffers.cuh:17-31,
+// sim/grid_buffers.cuh:8-28) where the meaning carries over, and adds the
+// cell-ordered arrays of the fused GB300 step.  Field meanings:
+//   d_pos, d_vel        committed state in ORIGINAL particle order (as the
+//                       reference's d_pos / d_vel)
+//   d_pos_pred          predicted positions in CELL order (sorted slots)
+//   d_pred_alt          second prediction buffer (Jacobi ping-pong; takes
+//                       the role of the reference's d_delta)
+//   d_pos_sorted        step-start positions in cell order
+//   d_vel_sorted        velocities in cell order (velocity phase output)
+//   d_lambda            lambda in cell order
+//   grid: d_cellKeys (id order), d_cellKeys_sorted, d_indices_sorted (sorted
+//   slot -> original id), d_cellLowerBound (numCells+1), compact table.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "parameters.h"
+
+namespace sim {
+
+struct DeviceBuffers {
+    float4* d_pos = nullptr;
+    float4* d_vel = nullptr;
+    float4* d_pos_pred = nullptr;
+    float4* d_pred_alt = nullptr;
+    float4* d_pos_sorted = nullptr;
+    float4* d_vel_sorted = nullptr;
+    float* d_lambda = nullptr;
+    float* d_lambda_by_id = nullptr;  // inspection only
+    DeviceParams* d_params = nullptr;  // device-resident parameter block
+    uint32_t* d_err = nullptr;         // device error word (bounded waits)
+    double* d_stats = nullptr;         // 4 results + per-block partials
+    uint32_t capacity = 0;
+    bool xsphEnabled = false;  // XSPH post-op configured at initialize (sim/simulator.cpp:277-285)
+
+    bool allocate(uint32_t cap);
+    void release();
+    ~DeviceBuffers() { release(); }
+};
+
+struct GridBuffers {
+    uint32_t* d_cellKeys = nullptr;
+    uint32_t* d_cellKeys_sorted = nullptr;
+    uint32_t* d_indices_sorted = nullptr;
+    uint32_t* d_cellLowerBound = nullptr;  // numCells + 1
+    uint32_t* d_cellStart = nullptr;       // reference dense format, materialised on request
+    uint32_t* d_cellEnd = nullptr;
+    uint32_t* d_cellUniqueKeys = nullptr;
+    uint32_t* d_cellOffsets = nullptr;  // capacity + 1
+    uint32_t* d_compactCount = nullptr;
+    void* d_sortTemp = nullptr;
+    size_t sortTempBytes = 0;
+    void* d_compactTemp = nullptr;
+    size_t compactTempBytes = 0;
+    uint32_t capacity = 0;
+    uint32_t numCells = 0;
+    int keyBits = 1;
+    bool hashed = false;
+
+    bool allocate(uint32_t cap, uint32_t nCells);
+    bool ensureRangesMaterialised();
+    void release();
+    ~GridBuffers() { release(); }
+};
+
+class KernelDispatcher;
+
+// sim/simulation_context.h:8-20
+struct SimulationContext {
+    DeviceBuffers* bufs = nullptr;
+    GridBuffers* grid = nullptr;
+    bool useHashedGrid = false;
+    KernelDispatcher* dispatcher = nullptr;
+};
+
+}  // namespace sim

@@ -1,0 +1,254 @@
+/*
+ * pbf.h - C ABI of the GB300 PBF step library (libpbf_gb300.so).
+ *
+ * Three layers, all extern "C", plain pointers and sizes, no C++ or torch
+ * types:
+ *
+ *  1. Phase launchers  pbf_launch_*  - one per reference launcher, same
+ *     argument order and meaning as the reference's extern "C" Launch*
+ *     functions (cited per entry), returning a status code instead of void.
+ *     Buffers use the reference's layout: particle arrays indexed by the
+ *     original particle id, neighbour tables indexed through indicesSorted.
+ *     The exact reference symbol names (LaunchHashKeys, ...) are exported too,
+ *     see launch_abi.h.
+ *  2. Whole-step handle  pbf_create / pbf_step / ...  - the fused GB300 step
+ *     (the reference's sim::Simulator::step, sim/simulator.cpp:560-643, with
+ *     the commit swap of :144-159 folded in).
+ *  3. Helpers: parameter construction (console::BuildSimParams semantics,
+ *     engine/core/console.cpp:198-267), seeded scene generation.
+ *
+ * Every call returns pbf_status (0 = PBF_OK).  No call aborts or traps.
+ * All device pointers are caller-owned unless stated otherwise; launchers
+ * never allocate.  Stream arguments are cudaStream_t (0 = legacy default).
+ */
+#ifndef PBF_H
+#define PBF_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+#include "pbf_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum pbf_status {
+    PBF_OK = 0,
+    PBF_ERR_INVALID = 1,     /* bad argument / size / aliasing */
+    PBF_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    PBF_ERR_OOM = 3,         /* device or host allocation failed */
+    PBF_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    PBF_ERR_NONFINITE = 5,   /* NaN/Inf detected in particle state */
+    PBF_ERR_UNSUPPORTED = 6  /* feature/size outside what this build handles */
+} pbf_status;
+
+const char* pbf_status_string(int status);
+int pbf_version(void); /* major*10000 + minor*100 + patch */
+/* sizeof of pbf_kernel_coeffs, pbf_grid_bounds, pbf_tuning, pbf_sim_params,
+ * pbf_device_params as compiled into the library (ABI check for bindings). */
+void pbf_abi_sizes(uint32_t out[5]);
+
+/* -------------------------------------------------------------- parameters */
+/* Defaults of sim::PbfTuning (reference sim/parameters.h:27-57). */
+void pbf_default_tuning(pbf_tuning* out);
+/* sim::MakeKernelCoeffs (sim/parameters.h:94-107). */
+void pbf_make_kernel_coeffs(float h, pbf_kernel_coeffs* out);
+/* sim::MakeDeviceParams (sim/parameters.h:109-123). */
+void pbf_make_device_params(const pbf_sim_params* sp, pbf_device_params* out);
+/* GridSystem::ComputeDims (sim/grid_system.h:9-17): ceil(extent/cellSize). */
+void pbf_compute_dims(const pbf_grid_bounds* g, int32_t out_dim[3]);
+
+/* Dam-break scene constants used by every plain-path configuration:
+ * particle radius r = 0.005, lattice spacing 0.01 = 2r, h = 2.5f*r,
+ * cell = h, rest density from the unjittered lattice (self term excluded,
+ * sim/pbf_lambda.cu:63), mass = 1000 * spacing^3, dt = 1/120, gravity
+ * (0,-9.8,0), lambda_denom_eps = 100, s_corr k=0.1 n=4 dq=0.2h, XSPH c=0.01,
+ * XPBD off, maxNeighbors 64, restitution 0; box [0, box_max].
+ * num_particles is stored in numParticles/maxParticles. */
+int pbf_dam_break_params(float box_max_x, float box_max_y, float box_max_z,
+                         int solver_iters, uint32_t num_particles,
+                         pbf_sim_params* out);
+
+/* Seeded lattice of nx*ny*nz particles at origin + (ix,iy,iz)*spacing with a
+ * per-axis uniform jitter in [-jitter, +jitter] drawn from
+ * std::mt19937_64(seed) (3 draws per particle, x,y,z), clamped into
+ * [box_min, box_max]; w = 1.  Particle order: x fastest, then y, then z
+ * (as sim::Simulator::seedBoxLattice, sim/simulator.cpp:831-846).
+ * pos_out must hold nx*ny*nz float4 (host memory). */
+int pbf_seed_lattice(float4* pos_out, uint32_t nx, uint32_t ny, uint32_t nz,
+                     float origin_x, float origin_y, float origin_z,
+                     float spacing, float jitter, uint64_t seed,
+                     const pbf_grid_bounds* clamp_box);
+
+/* ------------------------------------------------------- phase launchers */
+/* sim/integrate.cu:76-89 LaunchIntegratePred: posPred = pos + (vel + g dt) dt,
+ * posPred.w = pos.w. */
+int pbf_launch_integrate_pred(const float4* posCurr, const float4* velSrc,
+                              float4* posPred, float3 gravity, float dt,
+                              uint32_t N, cudaStream_t s);
+/* sim/boundary.cu:37-40 LaunchBoundary: clamp into the AABB, reflect the
+ * offending velocity component by -restitution, pos.w = 1, vel.w = 0. */
+int pbf_launch_boundary(float4* pos_pred, float4* vel, const pbf_grid_bounds* grid,
+                        float restitution, uint32_t N, cudaStream_t s);
+/* sim/boundary.cu:41-44 LaunchVelocity: vel = (pos_pred - pos) * inv_dt, w = 0. */
+int pbf_launch_velocity(float4* vel, const float4* pos, const float4* pos_pred,
+                        float inv_dt, uint32_t N, cudaStream_t s);
+/* sim/hash_keys.cu:30-34 LaunchHashKeys: keys[i] = clamped linear cell of
+ * pos[i], indices[i] = i. */
+int pbf_launch_hash_keys(uint32_t* keys, uint32_t* indices, const float4* pos,
+                         const pbf_grid_bounds* grid, uint32_t N, cudaStream_t s);
+
+/* sim/sort_pairs.cu:5-16 LaunchSortPairsQuery: temp bytes for N pairs. */
+int pbf_sort_pairs_query(size_t* tempBytes, uint32_t N);
+/* sim/sort_pairs.cu:18-27 LaunchSortPairs: stable ascending sort of
+ * (keys_in, vals_in) over key bits [0,32) into (keys_out, vals_out), by a
+ * onesweep LSD radix sort (8-bit digits, decoupled look-back).  Passes whose
+ * digit is the same for every key are skipped.  The inputs are left intact. */
+int pbf_launch_sort_pairs(void* d_temp, size_t tempBytes,
+                          const uint32_t* keys_in, uint32_t* keys_out,
+                          const uint32_t* vals_in, uint32_t* vals_out,
+                          uint32_t N, cudaStream_t s);
+/* Same sort restricted to key bits [0, num_bits). */
+int pbf_launch_sort_pairs_bits(void* d_temp, size_t tempBytes,
+                               const uint32_t* keys_in, uint32_t* keys_out,
+                               const uint32_t* vals_in, uint32_t* vals_out,
+                               uint32_t N, int num_bits, cudaStream_t s);
+
+/* sim/cell_ranges.cu:55-80 LaunchCellRanges: dense per-cell [start, end);
+ * empty cells get start = 0xFFFFFFFF, end = 0.  Writes every cell (no
+ * separate memsets needed). */
+int pbf_launch_cell_ranges(uint32_t* cellStart, uint32_t* cellEnd,
+                           const uint32_t* keysSorted, uint32_t N,
+                           uint32_t numCells, cudaStream_t s);
+
+/* Scratch for pbf_launch_cell_ranges_compact (replaces the reference's
+ * process-global scratch of sim/cell_compact.cu:50-93). */
+int pbf_cell_compact_scratch_query(size_t* bytes, uint32_t N);
+/* sim/cell_compact.cu:187-231 LaunchCellRangesCompact: uniqueKeys[m],
+ * offsets[m] = first sorted position of segment m, offsets[M] = N,
+ * *compactCount = M.  Segment starts are found with __match_any_sync and
+ * placed with a single-pass decoupled look-back scan. */
+int pbf_launch_cell_ranges_compact(void* d_scratch, size_t scratchBytes,
+                                   uint32_t* uniqueKeys, uint32_t* offsets,
+                                   uint32_t* compactCount,
+                                   const uint32_t* keysSorted, uint32_t N,
+                                   cudaStream_t s);
+
+/* sim/pbf_lambda.cu:246-258 LaunchLambda (dense table).  lambda[i] for every
+ * particle i; the reference writes through device globals bound to the same
+ * buffers, this entry point uses its arguments. */
+int pbf_launch_lambda(float* lambda, const float4* pos_pred,
+                      const uint32_t* indicesSorted, const uint32_t* keysSorted,
+                      const uint32_t* cellStart, const uint32_t* cellEnd,
+                      const pbf_device_params* dp, uint32_t N, cudaStream_t s);
+/* sim/pbf_lambda.cu:260-274 LaunchLambdaCompact (compact table). */
+int pbf_launch_lambda_compact(float* lambda, const float4* pos_pred,
+                              const uint32_t* indicesSorted, const uint32_t* keysSorted,
+                              const uint32_t* uniqueKeys, const uint32_t* offsets,
+                              const uint32_t* compactCount,
+                              const pbf_device_params* dp, uint32_t N, cudaStream_t s);
+/* sim/pbf_delta_apply.cu:239-258 LaunchDeltaApply: delta[i] then pos_pred += delta. */
+int pbf_launch_delta_apply(float4* pos_pred, float4* delta, const float* lambda,
+                           const uint32_t* indicesSorted, const uint32_t* keysSorted,
+                           const uint32_t* cellStart, const uint32_t* cellEnd,
+                           const pbf_device_params* dp, uint32_t N, cudaStream_t s);
+/* sim/pbf_delta_apply.cu:260-280 LaunchDeltaApplyCompact. */
+int pbf_launch_delta_apply_compact(float4* pos_pred, float4* delta, const float* lambda,
+                                   const uint32_t* indicesSorted, const uint32_t* keysSorted,
+                                   const uint32_t* uniqueKeys, const uint32_t* offsets,
+                                   const uint32_t* compactCount,
+                                   const pbf_device_params* dp, uint32_t N, cudaStream_t s);
+/* sim/xsph.cu:189-205 LaunchXSPH, Jacobi form: vel_out must not alias vel_in
+ * (PBF_ERR_INVALID otherwise).  No-op when dp->xsph_c <= 0. */
+int pbf_launch_xsph(float4* vel_out, const float4* vel_in, const float4* pos_pred,
+                    const uint32_t* indicesSorted, const uint32_t* keysSorted,
+                    const uint32_t* cellStart, const uint32_t* cellEnd,
+                    const pbf_device_params* dp, uint32_t N, cudaStream_t s);
+/* sim/xsph.cu:207-228 LaunchXSPHCompact, Jacobi form. */
+int pbf_launch_xsph_compact(float4* vel_out, const float4* vel_in, const float4* pos_pred,
+                            const uint32_t* indicesSorted, const uint32_t* keysSorted,
+                            const uint32_t* uniqueKeys, const uint32_t* offsets,
+                            const uint32_t* compactCount,
+                            const pbf_device_params* dp, uint32_t N, cudaStream_t s);
+
+/* ------------------------------------------------------ whole-step handle */
+typedef struct pbf_sim pbf_sim;
+
+/* Grid strategy: PBF_GRID_DENSE = per-cell start/end table
+ * (sim/phases.cpp:56-60), PBF_GRID_HASHED = compact unique-key table
+ * (console perf.use_hashed_grid, sim/phases.cpp:54). */
+enum { PBF_GRID_DENSE = 0, PBF_GRID_HASHED = 1 };
+
+/* sim::Simulator::initialize (sim/simulator.cpp:217-296): allocates every
+ * buffer for max(numParticles, maxParticles) particles and the grid of
+ * p->grid (dims recomputed with ComputeDims).  Owns a non-blocking stream. */
+int pbf_create(const pbf_sim_params* p, int grid_mode, pbf_sim** out);
+int pbf_destroy(pbf_sim* sim);
+/* The handle's stream (cudaStream_t). */
+void* pbf_stream(pbf_sim* sim);
+/* Device pointers of the committed state (float4[N], original particle order). */
+int pbf_device_state(pbf_sim* sim, float4** d_pos, float4** d_vel);
+
+/* Host <-> device state copies (blocking).  N = numParticles of the handle. */
+int pbf_upload_state(pbf_sim* sim, const float4* h_pos, const float4* h_vel);
+int pbf_download_state(pbf_sim* sim, float4* h_pos, float4* h_vel);
+
+/* One simulation step (sim::Simulator::step): launch the captured step graph
+ * on the handle's stream, asynchronously.  p may be NULL (parameters
+ * unchanged); a structural change (numParticles, solverIters, maxNeighbors,
+ * grid) re-captures the graph, any other change is uploaded to the
+ * device-resident parameter block before the launch. */
+int pbf_step(pbf_sim* sim, const pbf_sim_params* p);
+/* n steps back to back (same parameters). */
+int pbf_step_n(pbf_sim* sim, const pbf_sim_params* p, int n);
+/* End-to-end step on HOST buffers: copy h_pos/h_vel to the device, one step,
+ * copy the new state back, synchronize.  h_pos/h_vel should be pinned. */
+int pbf_step_host(pbf_sim* sim, const pbf_sim_params* p, float4* h_pos, float4* h_vel);
+/* One step launched phase by phase (not as a graph) with CUDA events between
+ * the launches, on the handle's stream; advances the state like pbf_step.
+ * Writes up to cap entries: ms[k] = device time of phase k, names[k] = its
+ * name (static strings); *count = number of phases (predict_keys, sort,
+ * gather_tables, lambda_1, delta_1, ..., commit). */
+int pbf_profile_step(pbf_sim* sim, const pbf_sim_params* p, float* ms, const char** names, int cap, int* count);
+/* Kernel launches of this library in one pbf_step (graph nodes that are
+ * kernels of libpbf_gb300; memsets excluded). */
+int pbf_launches_per_step(pbf_sim* sim);
+/* Wait for the stream and report any device-side error flag
+ * (PBF_ERR_TIMEOUT when a bounded wait gave up). */
+int pbf_synchronize(pbf_sim* sim);
+
+/* Density-constraint diagnostics of the committed state, uncapped neighbour
+ * sums over the step's cell grid: out[0] = mean |rho_i/rho0 - 1|,
+ * out[1] = max |rho_i/rho0 - 1|, out[2] = mean max(rho_i/rho0 - 1, 0),
+ * out[3] = mean neighbour count.  Deterministic (fixed-order reduction). */
+int pbf_density_stats(pbf_sim* sim, double out[4]);
+
+/* Test/inspection access to the last step's intermediates (blocking copy to
+ * host).  See PBF_DBG_*; bytes must match the item's size. */
+enum {
+    PBF_DBG_KEYS_SORTED = 0,   /* uint32[N] cell key per sorted slot */
+    PBF_DBG_PERM = 1,          /* uint32[N] original id per sorted slot */
+    PBF_DBG_CELL_START = 2,    /* uint32[numCells] reference dense format */
+    PBF_DBG_CELL_END = 3,      /* uint32[numCells] */
+    PBF_DBG_UNIQUE_KEYS = 4,   /* uint32[N] (first compactCount valid; hashed) */
+    PBF_DBG_OFFSETS = 5,       /* uint32[N+1] (first compactCount+1 valid) */
+    PBF_DBG_COMPACT_COUNT = 6, /* uint32[1] */
+    PBF_DBG_LAMBDA = 7,        /* float[N] last iteration's lambda by original id */
+    PBF_DBG_NUM_CELLS = 8      /* uint32[1] */
+};
+int pbf_debug_fetch(pbf_sim* sim, int item, void* host_dst, size_t bytes);
+
+/* Failure-path self-test of the bounded device waits: one block polls a
+ * look-back status that nothing ever publishes.  After spin_limit polls the
+ * kernel records the timeout in its error word and returns, leaving the
+ * context usable.  d_scratch: caller-owned device memory of >= 16 bytes.
+ * Returns PBF_ERR_TIMEOUT when the wait gave up as designed. */
+int pbf_selftest_bounded_wait(uint32_t spin_limit, void* d_scratch);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* PBF_H */

@@ -1,0 +1,745 @@
+// pbf_oracle.cpp - CPU restatement of the reference PBF step (test checker).
+//
+// TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
+// CPU-baseline leg of bench.py; never by the product library.
+//
+// Build: g++ -O3 -std=c++17 -fopenmp -ffp-contract=off -shared -fPIC
+// (no fast-math, no contraction: results are identical on x86-64 and
+// aarch64).  Templated on the real type: float reproduces the reference's
+// FP32 arithmetic op for op, double is the FP64 oracle.
+#include "pbf_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <typename R>
+struct V3 {
+    R x, y, z;
+};
+
+template <typename R>
+struct V4 {
+    R x, y, z, w;
+};
+
+// Real-typed copy of pbf_device_params (float: the same values).
+template <typename R>
+struct P {
+    R h, h2, poly6, spiky;
+    V3<R> mins, maxs;
+    R cs;
+    int dimx, dimy, dimz;
+    V3<R> g;
+    R rest, dt, inv_dt, e, mass, xsph_c;
+    int maxNeighbors;
+    // tuning
+    int scorr_enable;
+    R scorr_k, scorr_n, scorr_dq_h, wq_min, scorr_min, grad_r_eps, lambda_denom_eps, compliance;
+    int enable_lambda_clamp;
+    R lambda_max_abs;
+    int enable_disp_clamp;
+    R disp_clamp_max_h;
+    int enable_relax;
+    R relax_omega;
+    int xsph_gate_enable, xsph_n_min, xsph_n_max;
+};
+
+template <typename R>
+P<R> make_p(const pbf_device_params& d) {
+    P<R> p{};
+    p.h = R(d.kernel.h);
+    p.h2 = R(d.kernel.h2);
+    p.poly6 = R(d.kernel.poly6);
+    p.spiky = R(d.kernel.spiky);
+    p.mins = {R(d.grid.mins.x), R(d.grid.mins.y), R(d.grid.mins.z)};
+    p.maxs = {R(d.grid.maxs.x), R(d.grid.maxs.y), R(d.grid.maxs.z)};
+    p.cs = R(d.grid.cellSize);
+    p.dimx = d.grid.dim.x;
+    p.dimy = d.grid.dim.y;
+    p.dimz = d.grid.dim.z;
+    p.g = {R(d.gravity.x), R(d.gravity.y), R(d.gravity.z)};
+    p.rest = R(d.restDensity);
+    p.dt = R(d.dt);
+    p.inv_dt = R(d.inv_dt);
+    p.e = R(d.boundaryRestitution);
+    p.mass = R(d.particleMass);
+    p.xsph_c = R(d.xsph_c);
+    p.maxNeighbors = d.maxNeighbors;
+    const pbf_tuning& t = d.pbf;
+    p.scorr_enable = t.scorr_enable;
+    p.scorr_k = R(t.scorr_k);
+    p.scorr_n = R(t.scorr_n);
+    p.scorr_dq_h = R(t.scorr_dq_h);
+    p.wq_min = R(t.wq_min);
+    p.scorr_min = R(t.scorr_min);
+    p.grad_r_eps = R(t.grad_r_eps);
+    p.lambda_denom_eps = R(t.lambda_denom_eps);
+    p.compliance = R(t.compliance);
+    p.enable_lambda_clamp = t.enable_lambda_clamp;
+    p.lambda_max_abs = R(t.lambda_max_abs);
+    p.enable_disp_clamp = t.enable_disp_clamp;
+    p.disp_clamp_max_h = R(t.disp_clamp_max_h);
+    p.enable_relax = t.enable_relax;
+    p.relax_omega = R(t.relax_omega);
+    p.xsph_gate_enable = t.xsph_gate_enable;
+    p.xsph_n_min = t.xsph_n_min;
+    p.xsph_n_max = t.xsph_n_max;
+    return p;
+}
+
+// FP64 oracle kernel constants are recomputed in double from the same h so
+// that poly6/spiky carry no FP32 rounding.
+P<double> make_p64(const pbf_device_params& d) {
+    P<double> p = make_p<double>(d);
+    const double pi = 3.14159265358979323846;
+    const double h = p.h;
+    p.h2 = h * h;
+    p.poly6 = 315.0 / (64.0 * pi * std::pow(h, 9));
+    p.spiky = 15.0 / (pi * std::pow(h, 6));
+    p.inv_dt = (p.dt > 0) ? 1.0 / p.dt : 0.0;
+    return p;
+}
+
+inline float4 f4(float x, float y, float z, float w) {
+    float4 r;
+    r.x = x; r.y = y; r.z = z; r.w = w;
+    return r;
+}
+
+inline float fma_r(float a, float b, float c) { return std::fmaf(a, b, c); }
+inline double fma_r(double a, double b, double c) { return std::fma(a, b, c); }
+
+// sim/integrate.cu:40-51 (KIntegratePred).  The GPU computes both
+// multiply-adds as single fused operations; fmaf reproduces them exactly.
+template <typename R>
+void integrate_pred_t(const V4<R>* pos, const V4<R>* vel, V4<R>* pred, V3<R> g, R dt, uint32_t N) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)N; ++i) {
+        V4<R> p = pos[i], v = vel[i];
+        R vx = fma_r(g.x, dt, v.x);
+        R vy = fma_r(g.y, dt, v.y);
+        R vz = fma_r(g.z, dt, v.z);
+        pred[i] = {fma_r(vx, dt, p.x), fma_r(vy, dt, p.y), fma_r(vz, dt, p.z), p.w};
+    }
+}
+
+// sim/boundary.cu:11-25 (KBoundary): min checks x,y,z then max checks x,y,z.
+template <typename R>
+void boundary_t(V4<R>* pred, V4<R>* vel, V3<R> mins, V3<R> maxs, R restitution, uint32_t N) {
+    R e = restitution;
+    if (e < R(0)) e = R(0);
+    if (e > R(1)) e = R(1);
+    // fminf(fmaxf(r,0),1) also maps NaN to 0
+    if (!(restitution == restitution)) e = R(0);
+    const R ne = -e;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)N; ++i) {
+        V4<R> p = pred[i], v = vel[i];
+        if (p.x < mins.x) { p.x = mins.x; v.x *= ne; }
+        if (p.y < mins.y) { p.y = mins.y; v.y *= ne; }
+        if (p.z < mins.z) { p.z = mins.z; v.z *= ne; }
+        if (p.x > maxs.x) { p.x = maxs.x; v.x *= ne; }
+        if (p.y > maxs.y) { p.y = maxs.y; v.y *= ne; }
+        if (p.z > maxs.z) { p.z = maxs.z; v.z *= ne; }
+        pred[i] = {p.x, p.y, p.z, R(1)};
+        vel[i] = {v.x, v.y, v.z, R(0)};
+    }
+}
+
+// sim/boundary.cu:28-34 (KVelocity).
+template <typename R>
+void velocity_t(V4<R>* vel, const V4<R>* pos, const V4<R>* pred, R inv_dt, uint32_t N) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)N; ++i) {
+        vel[i] = {(pred[i].x - pos[i].x) * inv_dt, (pred[i].y - pos[i].y) * inv_dt,
+                  (pred[i].z - pos[i].z) * inv_dt, R(0)};
+    }
+}
+
+inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// float -> int as the GPU's truncating conversion: NaN -> 0, saturating.
+template <typename R>
+inline int to_int_sat(R f) {
+    if (!(f == f)) return 0;
+    if (f >= R(2147483647.0)) return 2147483647;
+    if (f <= R(-2147483648.0)) return (-2147483647 - 1);
+    return (int)f;
+}
+
+// sim/hash_keys.cu:6-27 (linearIndex + KHash): IEEE divide, floor, clamp.
+template <typename R>
+void hash_keys_t(uint32_t* keys, uint32_t* idx, const V4<R>* pred, V3<R> mins, R cs, int dx, int dy,
+                 int dz, uint32_t N) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)N; ++i) {
+        R rx = (pred[i].x - mins.x) / cs;
+        R ry = (pred[i].y - mins.y) / cs;
+        R rz = (pred[i].z - mins.z) / cs;
+        int cx = clampi(to_int_sat(std::floor(rx)), 0, dx - 1);
+        int cy = clampi(to_int_sat(std::floor(ry)), 0, dy - 1);
+        int cz = clampi(to_int_sat(std::floor(rz)), 0, dz - 1);
+        keys[i] = (uint32_t)((cz * dy + cy) * dx + cx);
+        if (idx) idx[i] = (uint32_t)i;
+    }
+}
+
+// Reference cell lookups.  Dense: sim/phases.cpp + sim/cell_ranges.cu
+// semantics (start==0xFFFFFFFF or start>=end means empty).  Compact:
+// lower_bound on unique keys (sim/cuda_grid_utils.cuh:34-67).
+struct Table {
+    const uint32_t* start;
+    const uint32_t* end;
+    const uint32_t* uk;
+    const uint32_t* off;
+    uint32_t M;
+    bool lookup(uint32_t cidx, uint32_t& b, uint32_t& e) const {
+        if (!uk) {
+            b = start[cidx];
+            e = end[cidx];
+            return !(b == 0xFFFFFFFFu || b >= e);
+        }
+        if (M == 0) { b = e = 0; return false; }
+        uint32_t lo = 0, hi = M;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (uk[mid] < cidx) lo = mid + 1; else hi = mid;
+        }
+        if (lo >= M || uk[lo] != cidx) { b = e = 0; return false; }
+        b = off[lo];
+        e = off[lo + 1];
+        return b < e;
+    }
+};
+
+Table make_table(const oracle_table* t) {
+    Table tb{};
+    tb.start = t->start;
+    tb.end = t->end;
+    tb.uk = t->unique_keys;
+    tb.off = t->offsets;
+    tb.M = t->count;
+    return tb;
+}
+
+template <typename R>
+inline void decode(uint32_t key, const P<R>& p, int& cx, int& cy, int& cz) {
+    cx = int(key % uint32_t(p.dimx));
+    uint32_t kdx = key / uint32_t(p.dimx);
+    cy = int(kdx % uint32_t(p.dimy));
+    cz = int(kdx / uint32_t(p.dimy));
+}
+
+template <typename R>
+inline int reach_of(const P<R>& p) {
+    if (!(p.cs > R(0))) return 1;
+    int r = int(std::ceil(float(p.h) / float(p.cs)));  // ceilf(h / cs) in FP32
+    return r > 1 ? r : 1;
+}
+
+// Neighbour iteration in reference order (sim/pbf_lambda.cu:49-84): for a
+// particle in cell (cx,cy,cz): dz, dy, dx in [-reach, reach], cells outside
+// [0,dim) skipped, then k ascending over the cell's sorted range.  f returns
+// false to stop the whole walk.
+template <typename R, typename F>
+inline void for_candidates(int cx, int cy, int cz, int reach, const P<R>& p, const Table& tb, F&& f) {
+    for (int dz = -reach; dz <= reach; ++dz)
+        for (int dy = -reach; dy <= reach; ++dy)
+            for (int dx = -reach; dx <= reach; ++dx) {
+                int x = cx + dx, y = cy + dy, z = cz + dz;
+                if (x < 0 || y < 0 || z < 0 || x >= p.dimx || y >= p.dimy || z >= p.dimz) continue;
+                uint32_t cidx = (uint32_t)((z * p.dimy + y) * p.dimx + x);
+                uint32_t b, e;
+                if (!tb.lookup(cidx, b, e)) continue;
+                for (uint32_t k = b; k < e; ++k)
+                    if (!f(k)) return;
+            }
+}
+
+// sim/pbf_lambda.cu:10-108 (KLambdaGlobalsDense / Compact).
+template <typename R>
+void lambda_t(R* lambda, const V4<R>* pred, const uint32_t* idx, const uint32_t* keys, const Table& tb,
+              const P<R>& p, uint32_t N) {
+    const int reach = reach_of(p);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t s = 0; s < (int64_t)N; ++s) {
+        const uint32_t i = idx[s];
+        const V4<R> pi = pred[i];
+        int cx, cy, cz;
+        decode(keys[s], p, cx, cy, cz);
+        R density = 0, gx = 0, gy = 0, gz = 0, sumGrad2 = 0;
+        int contrib = 0;
+        const int cap = p.maxNeighbors;
+        const bool hasCap = cap > 0;
+        for_candidates(cx, cy, cz, reach, p, tb, [&](uint32_t k) -> bool {
+            if (hasCap && contrib >= cap) return false;
+            const uint32_t j = idx[k];
+            if (j == i) return true;
+            const V4<R> pj = pred[j];
+            R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            R r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 > p.h2) return true;
+            ++contrib;
+            R hr2 = p.h2 - r2;
+            density += p.mass * p.poly6 * hr2 * hr2 * hr2;
+            R r = std::sqrt(r2);
+            R r_safe = std::max(r, p.grad_r_eps);
+            R t = p.h - r;
+            R coeff = (R(-3) * p.spiky * (t * t) / r_safe);
+            R ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
+            gx += ax; gy += ay; gz += az;
+            sumGrad2 += ax * ax + ay * ay + az * az;
+            return true;
+        });
+        R gradSum2 = gx * gx + gy * gy + gz * gz;
+        R scale = (p.rest > R(0)) ? (p.mass / p.rest) : R(0);
+        R denom = (scale * scale) * (sumGrad2 + gradSum2) + p.lambda_denom_eps;
+        if (p.compliance > R(0) && p.dt > R(0)) denom += p.compliance / (p.dt * p.dt);
+        denom = std::max(denom, p.lambda_denom_eps);
+        R lam;
+        if (contrib < 2 || (sumGrad2 + gradSum2) < R(1e-12f)) {
+            lam = R(0);
+        } else {
+            R C = (p.rest > R(0)) ? (density / p.rest - R(1)) : R(0);
+            lam = -C / denom;
+            if (!std::isfinite(lam)) lam = R(0);
+            if (p.enable_lambda_clamp) {
+                if (std::fabs(lam) > p.lambda_max_abs) lam = std::copysign(p.lambda_max_abs, lam);
+            }
+        }
+        lambda[i] = lam;
+    }
+}
+
+inline float pow_r(float a, float b) { return std::pow(a, b); }
+inline double pow_r(double a, double b) { return std::pow(a, b); }
+
+// sim/pbf_delta_apply.cu:10-113 (KDeltaCompute) + :223-235 (KApplyDelta).
+template <typename R>
+void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* idx, const uint32_t* keys,
+                   const Table& tb, const P<R>& p, uint32_t N) {
+    const int reach = reach_of(p);
+    const R dq = p.scorr_dq_h * p.h;
+    const R hr2_q = p.h2 - dq * dq;
+    const R w_q = (hr2_q > R(0)) ? (p.poly6 * hr2_q * hr2_q * hr2_q) : p.wq_min;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t s = 0; s < (int64_t)N; ++s) {
+        const uint32_t i = idx[s];
+        const V4<R> pi = pred[i];
+        int cx, cy, cz;
+        decode(keys[s], p, cx, cy, cz);
+        R dx_ = 0, dy_ = 0, dz_ = 0;
+        for_candidates(cx, cy, cz, reach, p, tb, [&](uint32_t k) -> bool {
+            const uint32_t j = idx[k];
+            if (j == i) return true;
+            const V4<R> pj = pred[j];
+            R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            R r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 > p.h2) return true;
+            R r = std::sqrt(r2);
+            R t = p.h - r;
+            R r_safe = std::max(r, p.grad_r_eps);
+            R coeff = (R(-3) * p.spiky * (t * t) / r_safe);
+            R ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
+            R scorr = 0;
+            if (p.scorr_enable) {
+                R hr2 = p.h2 - r2;
+                R w = p.poly6 * hr2 * hr2 * hr2;
+                R ratio = (w_q > R(0)) ? (w / w_q) : R(0);
+                scorr = -p.scorr_k * pow_r(ratio, p.scorr_n);
+                if (p.scorr_min < R(0)) scorr = std::max(scorr, p.scorr_min);
+            }
+            R lij = (lambda[i] + lambda[j] + scorr);
+            dx_ += lij * ax;
+            dy_ += lij * ay;
+            dz_ += lij * az;
+            return true;
+        });
+        R invRest = (p.rest > R(0)) ? (R(1) / p.rest) : R(0);
+        R ex = invRest * dx_, ey = invRest * dy_, ez = invRest * dz_;
+        if (p.enable_relax) { ex *= p.relax_omega; ey *= p.relax_omega; ez *= p.relax_omega; }
+        if (p.enable_disp_clamp) {
+            R maxDisp = p.disp_clamp_max_h * p.h;
+            R maxDisp2 = maxDisp * maxDisp;
+            R len2 = ex * ex + ey * ey + ez * ez;
+            if (len2 > maxDisp2) {
+                R len = std::sqrt(len2);
+                R sc = maxDisp / (len + R(1e-20f));
+                ex *= sc; ey *= sc; ez *= sc;
+            }
+        }
+        delta[i] = {ex, ey, ez, R(0)};
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < (int64_t)N; ++s) {
+        const uint32_t i = idx[s];
+        V4<R> b = pred[i];
+        pred[i] = {b.x + delta[i].x, b.y + delta[i].y, b.z + delta[i].z, b.w};
+    }
+}
+
+// sim/xsph.cu:9-96 (KXSPH), Jacobi: reads vel_in only.
+template <typename R>
+void xsph_t(V4<R>* vel_out, const V4<R>* vel_in, const V4<R>* pred, const uint32_t* idx, const uint32_t* keys,
+            const Table& tb, const P<R>& p, uint32_t N) {
+    const int reach = reach_of(p);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t s = 0; s < (int64_t)N; ++s) {
+        const uint32_t i = idx[s];
+        const V4<R> pi = pred[i];
+        const V4<R> vi = vel_in[i];
+        int cx, cy, cz;
+        decode(keys[s], p, cx, cy, cz);
+        R sx = 0, sy = 0, sz = 0;
+        int count = 0;
+        for_candidates(cx, cy, cz, reach, p, tb, [&](uint32_t k) -> bool {
+            const uint32_t j = idx[k];
+            if (j == i) return true;
+            const V4<R> pj = pred[j];
+            R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            R r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 > p.h2) return true;
+            R hr2 = p.h2 - r2;
+            R w = p.poly6 * hr2 * hr2 * hr2;
+            const V4<R> vj = vel_in[j];
+            sx += (vj.x - vi.x) * w;
+            sy += (vj.y - vi.y) * w;
+            sz += (vj.z - vi.z) * w;
+            ++count;
+            return true;
+        });
+        R gate = 1;
+        if (p.xsph_gate_enable) {
+            int nMin = std::max(0, p.xsph_n_min);
+            int nMax = std::max(nMin + 1, p.xsph_n_max);
+            float t = (float(count) - float(nMin)) / float(nMax - nMin);
+            gate = R(std::min(1.f, std::max(0.f, t)));
+        }
+        R mor = (p.rest > R(0)) ? (p.mass / p.rest) : R(0);
+        R c = (p.xsph_c * gate) * mor;
+        vel_out[i] = {vi.x + c * sx, vi.y + c * sy, vi.z + c * sz, R(0)};
+    }
+}
+
+// Stable LSD radix sort of (key, value) over bits [0,32): the same order as
+// the reference's cub::DeviceRadixSort::SortPairs (sim/sort_pairs.cu:18-27).
+void sort_pairs_impl(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t N) {
+    std::vector<uint32_t> k0(kin, kin + N), v0(vin, vin + N), k1(N), v1(N);
+    for (int pass = 0; pass < 4; ++pass) {
+        const int sh = pass * 8;
+        size_t cnt[257] = {0};
+        for (uint32_t i = 0; i < N; ++i) cnt[((k0[i] >> sh) & 255u) + 1]++;
+        bool trivial = false;
+        for (int d = 0; d < 256; ++d)
+            if (cnt[d + 1] == N) trivial = true;
+        if (trivial) continue;
+        for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+        for (uint32_t i = 0; i < N; ++i) {
+            size_t pos = cnt[(k0[i] >> sh) & 255u]++;
+            k1[pos] = k0[i];
+            v1[pos] = v0[i];
+        }
+        k0.swap(k1);
+        v0.swap(v1);
+    }
+    std::memcpy(kout, k0.data(), sizeof(uint32_t) * N);
+    std::memcpy(vout, v0.data(), sizeof(uint32_t) * N);
+}
+
+// sim/cell_ranges.cu:21-51 with the memsets of sim/phases.cpp:58-59 and
+// sim/cell_ranges.cu:62-63 (start=0xFFFFFFFF, end=0 for empty cells).
+void cell_ranges_impl(uint32_t* start, uint32_t* end, const uint32_t* ks, uint32_t N, uint32_t numCells) {
+    for (uint32_t c = 0; c < numCells; ++c) { start[c] = 0xFFFFFFFFu; end[c] = 0u; }
+    for (uint32_t i = 0; i < N; ++i) {
+        uint32_t k = ks[i];
+        if (k >= numCells) continue;
+        if (i == 0) start[k] = 0;
+        else {
+            uint32_t kp = ks[i - 1];
+            if (k != kp) {
+                if (kp < numCells) end[kp] = i;
+                start[k] = i;
+            }
+        }
+        if (i == N - 1) end[k] = N;
+    }
+}
+
+// sim/cell_compact.cu:96-184 (flags, block scan, scatter + terminator).
+void cell_compact_impl(uint32_t* uk, uint32_t* off, uint32_t* count, const uint32_t* ks, uint32_t N) {
+    if (N == 0) { off[0] = 0; *count = 0; return; }
+    uint32_t m = 0;
+    for (uint32_t i = 0; i < N; ++i) {
+        if (i == 0 || ks[i] != ks[i - 1]) {
+            uk[m] = ks[i];
+            off[m] = i;
+            ++m;
+        }
+    }
+    off[m] = N;
+    *count = m;
+}
+
+inline const V4<float>* as4(const float4* p) { return reinterpret_cast<const V4<float>*>(p); }
+inline V4<float>* as4(float4* p) { return reinterpret_cast<V4<float>*>(p); }
+
+pbf_device_params device_params_of(const pbf_sim_params& sp) {
+    pbf_device_params dp{};
+    dp.kernel = sp.kernel;
+    dp.grid = sp.grid;
+    dp.gravity = sp.gravity;
+    dp.restDensity = sp.restDensity;
+    dp.dt = sp.dt;
+    dp.inv_dt = (sp.dt > 0.f) ? (1.0f / sp.dt) : 0.0f;
+    dp.boundaryRestitution = sp.boundaryRestitution;
+    dp.maxNeighbors = sp.maxNeighbors;
+    dp.particleMass = sp.particleMass;
+    dp.pbf = sp.pbf;
+    dp.xsph_c = sp.xsph_c;
+    return dp;
+}
+
+// GridSystem::ComputeDims (sim/grid_system.h:9-17).
+void compute_dims(pbf_grid_bounds& g) {
+    const float cs = (g.cellSize > 0.f) ? g.cellSize : 1.f;
+    int dx = int(std::ceil((g.maxs.x - g.mins.x) / cs));
+    int dy = int(std::ceil((g.maxs.y - g.mins.y) / cs));
+    int dz = int(std::ceil((g.maxs.z - g.mins.z) / cs));
+    g.dim.x = dx < 0 ? 0 : dx;
+    g.dim.y = dy < 0 ? 0 : dy;
+    g.dim.z = dz < 0 ? 0 : dz;
+}
+
+// One step in reference order, generic over the real type.
+template <typename R>
+int step_t(const pbf_sim_params& sp0, int hashed, V4<R>* pos, V4<R>* vel, uint32_t N, oracle_trace* tr,
+           const P<R>& p) {
+    pbf_sim_params sp = sp0;
+    compute_dims(sp.grid);
+    const uint32_t numCells = uint32_t(sp.grid.dim.x) * uint32_t(sp.grid.dim.y) * uint32_t(sp.grid.dim.z);
+    if (numCells == 0) return 1;
+    std::vector<V4<R>> pred(N), delta(N), vtmp(N);
+    std::vector<R> lam(N);
+    std::vector<uint32_t> keys(N), idx(N), ks(N), is(N);
+    // PhaseIntegrate (sim/phases.cpp:33-36)
+    integrate_pred_t<R>(pos, vel, pred.data(), p.g, p.dt, N);
+    boundary_t<R>(pred.data(), vel, p.mins, p.maxs, R(0), N);
+    // PhaseGridBuildFull (sim/phases.cpp:44-63)
+    hash_keys_t<R>(keys.data(), idx.data(), pred.data(), p.mins, p.cs, p.dimx, p.dimy, p.dimz, N);
+    sort_pairs_impl(keys.data(), ks.data(), idx.data(), is.data(), N);
+    std::vector<uint32_t> start, end, uk, off;
+    uint32_t M = 0;
+    Table tb{};
+    if (hashed) {
+        uk.resize(N > 0 ? N : 1);
+        off.resize(N + 1);
+        cell_compact_impl(uk.data(), off.data(), &M, ks.data(), N);
+        tb.uk = uk.data();
+        tb.off = off.data();
+        tb.M = M;
+    } else {
+        start.resize(numCells);
+        end.resize(numCells);
+        cell_ranges_impl(start.data(), end.data(), ks.data(), N, numCells);
+        tb.start = start.data();
+        tb.end = end.data();
+    }
+    // PhaseSolveIterations (sim/phases.cpp:71-94)
+    for (int it = 0; it < sp.solverIters; ++it) {
+        lambda_t<R>(lam.data(), pred.data(), is.data(), ks.data(), tb, p, N);
+        delta_apply_t<R>(pred.data(), delta.data(), lam.data(), is.data(), ks.data(), tb, p, N);
+    }
+    if (tr && tr->pred_solved) {
+        for (uint32_t i = 0; i < N; ++i)
+            tr->pred_solved[i] = f4(float(pred[i].x), float(pred[i].y), float(pred[i].z), float(pred[i].w));
+    }
+    boundary_t<R>(pred.data(), vel, p.mins, p.maxs, R(0), N);
+    // PhaseVelocity (sim/phases.cpp:102-105): inv_dt = 1.0f / p.dt
+    const R inv_dt = (sizeof(R) == 4) ? R(1.0f / sp.dt) : R(1.0) / R(p.dt);
+    velocity_t<R>(vel, pos, pred.data(), inv_dt, N);
+    if (tr && tr->vel_pre_xsph) {
+        for (uint32_t i = 0; i < N; ++i)
+            tr->vel_pre_xsph[i] = f4(float(vel[i].x), float(vel[i].y), float(vel[i].z), float(vel[i].w));
+    }
+    // PostOps XSPH -> Boundary -> Recycle (sim/post_ops.cpp:73-85)
+    if (sp.xsph_c > 0.f) {
+        xsph_t<R>(vtmp.data(), vel, pred.data(), is.data(), ks.data(), tb, p, N);
+        std::memcpy(vel, vtmp.data(), sizeof(V4<R>) * N);
+    }
+    boundary_t<R>(pred.data(), vel, p.mins, p.maxs, p.e, N);
+    // commit (ping-pong swap, sim/simulator.cpp:144-159)
+    std::memcpy(pos, pred.data(), sizeof(V4<R>) * N);
+    if (tr) {
+        if (tr->keys) std::memcpy(tr->keys, keys.data(), 4 * N);
+        if (tr->keys_sorted) std::memcpy(tr->keys_sorted, ks.data(), 4 * N);
+        if (tr->perm) std::memcpy(tr->perm, is.data(), 4 * N);
+        if (!hashed) {
+            if (tr->cell_start) std::memcpy(tr->cell_start, start.data(), 4 * size_t(numCells));
+            if (tr->cell_end) std::memcpy(tr->cell_end, end.data(), 4 * size_t(numCells));
+        } else {
+            if (tr->unique_keys) std::memcpy(tr->unique_keys, uk.data(), 4 * size_t(M));
+            if (tr->offsets) std::memcpy(tr->offsets, off.data(), 4 * size_t(M + 1));
+            if (tr->compact_count) *tr->compact_count = M;
+        }
+        if (tr->lambda)
+            for (uint32_t i = 0; i < N; ++i) tr->lambda[i] = float(lam[i]);
+    }
+    return 0;
+}
+
+// FP64 density statistics over positions given as doubles.
+void density_stats_impl(const pbf_sim_params& sp0, const double* xyz4, uint32_t N, double out[4]) {
+    pbf_sim_params sp = sp0;
+    compute_dims(sp.grid);
+    pbf_device_params dp = device_params_of(sp);
+    P<double> p = make_p64(dp);
+    const uint32_t numCells = uint32_t(sp.grid.dim.x) * uint32_t(sp.grid.dim.y) * uint32_t(sp.grid.dim.z);
+    std::vector<V4<double>> pos(N);
+    for (uint32_t i = 0; i < N; ++i) pos[i] = {xyz4[4 * i], xyz4[4 * i + 1], xyz4[4 * i + 2], 1.0};
+    std::vector<uint32_t> keys(N), idx(N), ks(N), is(N), start(numCells), end(numCells);
+    // Cells from the FP32 positions' own rounding rules, evaluated in double.
+    hash_keys_t<double>(keys.data(), idx.data(), pos.data(), p.mins, p.cs, p.dimx, p.dimy, p.dimz, N);
+    sort_pairs_impl(keys.data(), ks.data(), idx.data(), is.data(), N);
+    cell_ranges_impl(start.data(), end.data(), ks.data(), N, numCells);
+    Table tb{};
+    tb.start = start.data();
+    tb.end = end.data();
+    const int reach = reach_of(p);
+    double sumAbs = 0, maxAbs = 0, sumPos = 0, sumNb = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : sumAbs, sumPos, sumNb) reduction(max : maxAbs)
+    for (int64_t s = 0; s < (int64_t)N; ++s) {
+        const uint32_t i = is[s];
+        const V4<double> pi = pos[i];
+        int cx, cy, cz;
+        decode(ks[s], p, cx, cy, cz);
+        double rho = 0;
+        int nb = 0;
+        for_candidates(cx, cy, cz, reach, p, tb, [&](uint32_t k) -> bool {
+            const uint32_t j = is[k];
+            if (j == i) return true;
+            double rx = pi.x - pos[j].x, ry = pi.y - pos[j].y, rz = pi.z - pos[j].z;
+            double r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 > p.h2) return true;
+            double hr2 = p.h2 - r2;
+            rho += p.mass * p.poly6 * hr2 * hr2 * hr2;
+            ++nb;
+            return true;
+        });
+        double C = (p.rest > 0) ? rho / p.rest - 1.0 : 0.0;
+        sumAbs += std::fabs(C);
+        maxAbs = std::max(maxAbs, std::fabs(C));
+        sumPos += C > 0 ? C : 0.0;
+        sumNb += nb;
+    }
+    const double n = N > 0 ? double(N) : 1.0;
+    out[0] = sumAbs / n;
+    out[1] = maxAbs;
+    out[2] = sumPos / n;
+    out[3] = sumNb / n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void oracle_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+void oracle_integrate_pred(const float4* pos, const float4* vel, float4* pred, float3 g, float dt, uint32_t N) {
+    integrate_pred_t<float>(as4(pos), as4(vel), as4(pred), V3<float>{g.x, g.y, g.z}, dt, N);
+}
+
+void oracle_boundary(float4* pred, float4* vel, const pbf_grid_bounds* g, float restitution, uint32_t N) {
+    boundary_t<float>(as4(pred), as4(vel), V3<float>{g->mins.x, g->mins.y, g->mins.z},
+                      V3<float>{g->maxs.x, g->maxs.y, g->maxs.z}, restitution, N);
+}
+
+void oracle_velocity(float4* vel, const float4* pos, const float4* pred, float inv_dt, uint32_t N) {
+    velocity_t<float>(as4(vel), as4(pos), as4(pred), inv_dt, N);
+}
+
+void oracle_hash_keys(uint32_t* keys, uint32_t* indices, const float4* pred, const pbf_grid_bounds* g, uint32_t N) {
+    hash_keys_t<float>(keys, indices, as4(pred), V3<float>{g->mins.x, g->mins.y, g->mins.z}, g->cellSize,
+                       g->dim.x, g->dim.y, g->dim.z, N);
+}
+
+void oracle_sort_pairs(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t N) {
+    sort_pairs_impl(kin, kout, vin, vout, N);
+}
+
+void oracle_cell_ranges(uint32_t* start, uint32_t* end, const uint32_t* ks, uint32_t N, uint32_t numCells) {
+    cell_ranges_impl(start, end, ks, N, numCells);
+}
+
+void oracle_cell_ranges_compact(uint32_t* uk, uint32_t* off, uint32_t* count, const uint32_t* ks, uint32_t N) {
+    cell_compact_impl(uk, off, count, ks, N);
+}
+
+void oracle_lambda(float* lambda, const float4* pred, const uint32_t* idx, const uint32_t* keys,
+                   const oracle_table* t, const pbf_device_params* dp, uint32_t N) {
+    lambda_t<float>(lambda, as4(pred), idx, keys, make_table(t), make_p<float>(*dp), N);
+}
+
+void oracle_delta_apply(float4* pred, float4* delta, const float* lambda, const uint32_t* idx,
+                        const uint32_t* keys, const oracle_table* t, const pbf_device_params* dp, uint32_t N) {
+    delta_apply_t<float>(as4(pred), as4(delta), lambda, idx, keys, make_table(t), make_p<float>(*dp), N);
+}
+
+void oracle_xsph(float4* vel_out, const float4* vel_in, const float4* pred, const uint32_t* idx,
+                 const uint32_t* keys, const oracle_table* t, const pbf_device_params* dp, uint32_t N) {
+    xsph_t<float>(as4(vel_out), as4(vel_in), as4(pred), idx, keys, make_table(t), make_p<float>(*dp), N);
+}
+
+int oracle_step_f32(const pbf_sim_params* p, int hashed, float4* pos, float4* vel, uint32_t N,
+                    oracle_trace* trace) {
+    pbf_sim_params sp = *p;
+    compute_dims(sp.grid);
+    pbf_device_params dp = device_params_of(sp);
+    return step_t<float>(sp, hashed, as4(pos), as4(vel), N, trace, make_p<float>(dp));
+}
+
+int oracle_step_f64(const pbf_sim_params* p, int hashed, double* pos4, double* vel4, uint32_t N) {
+    pbf_sim_params sp = *p;
+    compute_dims(sp.grid);
+    pbf_device_params dp = device_params_of(sp);
+    return step_t<double>(sp, hashed, reinterpret_cast<V4<double>*>(pos4), reinterpret_cast<V4<double>*>(vel4),
+                          N, nullptr, make_p64(dp));
+}
+
+void oracle_density_stats_f32pos(const pbf_sim_params* p, const float4* pos, uint32_t N, double out[4]) {
+    std::vector<double> x(4 * size_t(N));
+    for (uint32_t i = 0; i < N; ++i) {
+        x[4 * i] = pos[i].x;
+        x[4 * i + 1] = pos[i].y;
+        x[4 * i + 2] = pos[i].z;
+        x[4 * i + 3] = 1.0;
+    }
+    density_stats_impl(*p, x.data(), N, out);
+}
+
+void oracle_density_stats_f64pos(const pbf_sim_params* p, const double* pos4, uint32_t N, double out[4]) {
+    density_stats_impl(*p, pos4, N, out);
+}
+
+}  // extern "C"
