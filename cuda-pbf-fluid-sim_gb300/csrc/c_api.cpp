@@ -511,6 +511,14 @@ int pbf_debug_fetch(pbf_sim* h, int item, void* dst, size_t bytes) {
     return from_cuda(cudaStreamSynchronize(s));
 }
 
+int pbf_debug_eval_math(int fn, const float* a, const float* b, float* out, uint32_t n) {
+    if (n == 0) return PBF_OK;
+    if (!a || !out || (fn != 1 && !b) || fn < 0 || fn > 2) return PBF_ERR_INVALID;
+    cudaError_t e = pbf::eval_math(fn, a, b, out, n, 0);
+    if (e != cudaSuccess) return from_cuda(e);
+    return from_cuda(cudaDeviceSynchronize());
+}
+
 int pbf_selftest_bounded_wait(uint32_t spin_limit, void* d_scratch) {
     if (!d_scratch) return PBF_ERR_INVALID;
     uint32_t* w = static_cast<uint32_t*>(d_scratch);

@@ -162,7 +162,29 @@ __global__ void k_selftest_lookback(const uint32_t* status, uint32_t spin_limit,
     if (threadIdx.x == 0) *out = v;
 }
 
+// Device math used by the neighbour kernels, evaluated on arrays (for
+// checking CPU restatements against the GPU's results).
+__global__ void k_eval_math(int fn, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out,
+                            uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float r;
+    switch (fn) {
+        case 0: r = powf(a[i], b[i]); break;
+        case 1: r = sqrtf(a[i]); break;
+        case 2: r = a[i] / b[i]; break;
+        default: r = 0.f; break;
+    }
+    out[i] = r;
+}
+
 }  // namespace
+
+cudaError_t eval_math(int fn, const float* a, const float* b, float* out, uint32_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_eval_math<<<blocks_for(n, 256), 256, 0, s>>>(fn, a, b, out, n);
+    return cudaGetLastError();
+}
 
 cudaError_t selftest_bounded_wait(uint32_t spin_limit, uint32_t* d_scratch4, cudaStream_t s) {
     // d_scratch4: [0] status of tile 0 (kept 0 = never published), [1] err, [2] out

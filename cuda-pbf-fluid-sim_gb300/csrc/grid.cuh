@@ -35,6 +35,9 @@ cudaError_t launch_compact(void* d_scratch, size_t scratch_bytes, uint32_t* uniq
                            uint32_t* count, uint32_t* seg, const uint32_t* keys_sorted, uint32_t N, cudaStream_t s,
                            uint32_t* err);
 
+// Device powf (fn 0), sqrtf (fn 1), division (fn 2) on arrays.
+cudaError_t eval_math(int fn, const float* a, const float* b, float* out, uint32_t n, cudaStream_t s);
+
 // Bounded-wait self-test (see pbf_selftest_bounded_wait).
 cudaError_t selftest_bounded_wait(uint32_t spin_limit, uint32_t* d_scratch4, cudaStream_t s);
 

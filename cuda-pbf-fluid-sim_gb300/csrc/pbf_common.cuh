@@ -253,15 +253,8 @@ __device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int
     return lam;
 }
 
-// s_corr exponent: n == 4 (every configuration here) is evaluated as
-// (ratio^2)^2, which differs from powf by at most a couple of ulps.
-__device__ __forceinline__ float scorr_pow(float ratio, float n) {
-    if (n == 4.0f) {
-        const float r2 = ratio * ratio;
-        return r2 * r2;
-    }
-    return powf(ratio, n);
-}
+// s_corr exponent: powf, as the reference (sim/pbf_delta_apply.cu:82).
+__device__ __forceinline__ float scorr_pow(float ratio, float n) { return powf(ratio, n); }
 
 // w_q of the tensile-instability term (sim/pbf_delta_apply.cu:40-42).
 __device__ __forceinline__ float scorr_wq(const sim::DeviceParams& dp) {

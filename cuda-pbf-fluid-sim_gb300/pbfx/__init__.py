@@ -15,6 +15,8 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ROOT = os.path.dirname(PKG_DIR)
 LIB_PATH = os.path.join(PKG_DIR, "lib", "libpbf_gb300.so")
 ORACLE_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+REF_HARNESS_PATH = os.path.join(ROOT, "oracle", "_build", "libref_harness.so")
+REF_IMAGES = os.path.join(ROOT, "oracle", "_ref")
 
 PBF_OK = 0
 PBF_ERR_INVALID = 1
@@ -140,6 +142,7 @@ _SIGS = {
     "pbf_density_stats": ([_VP, C.POINTER(C.c_double * 4)], _I),
     "pbf_debug_fetch": ([_VP, _I, _VP, _SZ], _I),
     "pbf_selftest_bounded_wait": ([_U32, _VP], _I),
+    "pbf_debug_eval_math": ([_I, _VP, _VP, _VP, _U32], _I),
     "pbf_profile_step": ([_VP, C.POINTER(SimParams), C.POINTER(C.c_float), C.POINTER(C.c_char_p), _I,
                           C.POINTER(_I)], _I),
     "pbf_launches_per_step": ([_VP], _I),
@@ -173,8 +176,21 @@ def _bind(lib, sigs):
     return lib
 
 
+_REF_SIGS = {
+    "ref_init": ([C.c_char_p], _I),
+    "ref_error": ([], C.c_char_p),
+    "ref_step": ([C.POINTER(SimParams), _I, _VP, _VP, _U32, C.POINTER(OracleTrace)], _I),
+    "ref_time_steps": ([C.POINTER(SimParams), _I, _VP, _VP, _U32, _I, _I, C.POINTER(C.c_double)], _I),
+    "ref_phase_lambda": ([_VP, _VP, _VP, _VP, C.POINTER(OracleTable), C.POINTER(DeviceParams), _U32, _U32], _I),
+    "ref_phase_delta_apply": ([_VP, _VP, _VP, _VP, _VP, C.POINTER(OracleTable), C.POINTER(DeviceParams), _U32, _U32],
+                              _I),
+    "ref_phase_xsph": ([_VP, _VP, _VP, _VP, _VP, C.POINTER(OracleTable), C.POINTER(DeviceParams), _U32, _U32], _I),
+    "ref_phase_integrate_boundary": ([_VP, _VP, _VP, C.POINTER(SimParams), _U32], _I),
+}
+
 _lib = None
 _oracle = None
+_ref = None
 
 
 def load(path: str = LIB_PATH):
@@ -195,6 +211,21 @@ def load_oracle(path: str = ORACLE_PATH):
             raise RuntimeError("oracle not built: run __graft_entry__.build()")
         _oracle = _bind(C.CDLL(path), _ORACLE_SIGS)
     return _oracle
+
+
+def load_ref():
+    """The reference's own kernels driven by oracle/ref/ref_harness.cu (test
+    infrastructure only), or None when its device images are not present."""
+    global _ref
+    if _ref is None:
+        imgs = os.path.join(REF_IMAGES, "pbf_lambda.cubin")
+        if not (os.path.exists(REF_HARNESS_PATH) and os.path.exists(imgs)):
+            return None
+        lib = _bind(C.CDLL(REF_HARNESS_PATH), _REF_SIGS)
+        if lib.ref_init(REF_IMAGES.encode()) != 0:
+            raise RuntimeError("reference harness: %s" % lib.ref_error().decode())
+        _ref = lib
+    return _ref
 
 
 def check(status: int, what: str = "call"):
@@ -317,6 +348,16 @@ class Sim:
 
 def oracle_step(orc, params: SimParams, hashed: bool, pos: np.ndarray, vel: np.ndarray, trace: bool = True):
     """One FP32 oracle step in place; returns the trace arrays."""
+    return _traced_step(orc.oracle_step_f32, params, hashed, pos, vel, trace)
+
+
+def ref_step(ref, params: SimParams, hashed: bool, pos: np.ndarray, vel: np.ndarray, trace: bool = True):
+    """One step of the reference's own kernels in place; returns the trace
+    (keys, sorted keys, permutation, cell tables, lambda)."""
+    return _traced_step(ref.ref_step, params, hashed, pos, vel, trace, gpu_ref=True)
+
+
+def _traced_step(fn, params, hashed, pos, vel, trace, gpu_ref=False):
     n = int(pos.shape[0])
     nc = num_cells(params)
     tr = {}
@@ -336,9 +377,14 @@ def oracle_step(orc, params: SimParams, hashed: bool, pos: np.ndarray, vel: np.n
             tr["cell_end"] = np.zeros(nc, np.uint32)
         for k, v in tr.items():
             setattr(t, "lambda_" if k == "lambda" else k, v.ctypes.data)
-    rc = orc.oracle_step_f32(C.byref(params), 1 if hashed else 0, ptr(pos), ptr(vel), n, C.byref(t) if trace else None)
+    if gpu_ref:
+        t.pred_solved = None
+        t.vel_pre_xsph = None
+        tr.pop("pred_solved", None)
+        tr.pop("vel_pre_xsph", None)
+    rc = fn(C.byref(params), 1 if hashed else 0, ptr(pos), ptr(vel), n, C.byref(t) if trace else None)
     if rc != 0:
-        raise RuntimeError("oracle_step_f32 failed")
+        raise RuntimeError("step failed (%d)" % rc)
     if trace and hashed:
         m = int(tr["compact_count"][0])
         tr["unique_keys"] = tr["unique_keys"][:m]

@@ -240,6 +240,10 @@ enum {
 };
 int pbf_debug_fetch(pbf_sim* sim, int item, void* host_dst, size_t bytes);
 
+/* Inspection: evaluates the device math the neighbour kernels use on
+ * device arrays: fn 0 = powf(a, b), 1 = sqrtf(a), 2 = a / b (IEEE). */
+int pbf_debug_eval_math(int fn, const float* d_a, const float* d_b, float* d_out, uint32_t n);
+
 /* Failure-path self-test of the bounded device waits: one block polls a
  * look-back status that nothing ever publishes.  After spin_limit polls the
  * kernel records the timeout in its error word and returns, leaving the

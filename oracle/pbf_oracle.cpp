@@ -4,9 +4,25 @@
 // CPU-baseline leg of bench.py; never by the product library.
 //
 // Build: g++ -O3 -std=c++17 -fopenmp -ffp-contract=off -shared -fPIC
-// (no fast-math, no contraction: results are identical on x86-64 and
-// aarch64).  Templated on the real type: float reproduces the reference's
-// FP32 arithmetic op for op, double is the FP64 oracle.
+// (no fast-math, no implicit contraction: results are identical on x86-64
+// and aarch64).  Templated on the real type: float reproduces the
+// reference's FP32 arithmetic op for op, double is the FP64 oracle.
+//
+// FMA contraction.  nvcc (default -fmad=true) fuses some multiply-adds of the
+// reference kernels; the fused operations are written out here as explicit
+// fma calls, so the FP32 oracle reproduces the reference kernels bit for bit.
+// The fused sites were identified by comparing candidate forms against the
+// reference kernels' outputs on the GPU (32,768 particles, lattice and
+// compressed states; every lambda and XSPH velocity bit-identical):
+//   r^2 = fma(rz, rz, fma(rx, rx, ry*ry))               all neighbour loops
+//   density = fma(m*poly6*hr2*hr2, hr2, density)         lambda
+//   sumGrad2 = sumGrad2 + fma(az, az, fma(ax, ax, ay*ay)) lambda (gradSum += a unfused)
+//   |gradSum|^2 like r^2; denom = fma(scale*scale, sum, eps)
+//   dx = fma(lij, ax, dx); |d|^2 like r^2;  w_q: h2 - dq*dq = fma(-dq, dq, h2)   delta
+//   sum = fma(vj - vi, W, sum); v = fma(c*gate*m/rho0, sum, vi)                  XSPH
+// The one operation the oracle cannot reproduce exactly is CUDA's powf (the
+// s_corr exponent), which is not correctly rounded; the oracle uses the C
+// library's powf, so position corrections agree to rounding, not bitwise.
 #include "pbf_oracle.h"
 
 #include <algorithm>
@@ -285,23 +301,23 @@ void lambda_t(R* lambda, const V4<R>* pred, const uint32_t* idx, const uint32_t*
             if (j == i) return true;
             const V4<R> pj = pred[j];
             R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            R r2 = rx * rx + ry * ry + rz * rz;
+            R r2 = fma_r(rz, rz, fma_r(rx, rx, ry * ry));
             if (r2 > p.h2) return true;
             ++contrib;
             R hr2 = p.h2 - r2;
-            density += p.mass * p.poly6 * hr2 * hr2 * hr2;
+            density = fma_r(p.mass * p.poly6 * hr2 * hr2, hr2, density);
             R r = std::sqrt(r2);
             R r_safe = std::max(r, p.grad_r_eps);
             R t = p.h - r;
             R coeff = (R(-3) * p.spiky * (t * t) / r_safe);
             R ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
             gx += ax; gy += ay; gz += az;
-            sumGrad2 += ax * ax + ay * ay + az * az;
+            sumGrad2 = sumGrad2 + fma_r(az, az, fma_r(ax, ax, ay * ay));
             return true;
         });
-        R gradSum2 = gx * gx + gy * gy + gz * gz;
+        R gradSum2 = fma_r(gz, gz, fma_r(gx, gx, gy * gy));
         R scale = (p.rest > R(0)) ? (p.mass / p.rest) : R(0);
-        R denom = (scale * scale) * (sumGrad2 + gradSum2) + p.lambda_denom_eps;
+        R denom = fma_r(scale * scale, sumGrad2 + gradSum2, p.lambda_denom_eps);
         if (p.compliance > R(0) && p.dt > R(0)) denom += p.compliance / (p.dt * p.dt);
         denom = std::max(denom, p.lambda_denom_eps);
         R lam;
@@ -328,7 +344,7 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
                    const Table& tb, const P<R>& p, uint32_t N) {
     const int reach = reach_of(p);
     const R dq = p.scorr_dq_h * p.h;
-    const R hr2_q = p.h2 - dq * dq;
+    const R hr2_q = fma_r(-dq, dq, p.h2);
     const R w_q = (hr2_q > R(0)) ? (p.poly6 * hr2_q * hr2_q * hr2_q) : p.wq_min;
 #pragma omp parallel for schedule(dynamic, 1024)
     for (int64_t s = 0; s < (int64_t)N; ++s) {
@@ -342,7 +358,7 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
             if (j == i) return true;
             const V4<R> pj = pred[j];
             R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            R r2 = rx * rx + ry * ry + rz * rz;
+            R r2 = fma_r(rz, rz, fma_r(rx, rx, ry * ry));
             if (r2 > p.h2) return true;
             R r = std::sqrt(r2);
             R t = p.h - r;
@@ -358,9 +374,9 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
                 if (p.scorr_min < R(0)) scorr = std::max(scorr, p.scorr_min);
             }
             R lij = (lambda[i] + lambda[j] + scorr);
-            dx_ += lij * ax;
-            dy_ += lij * ay;
-            dz_ += lij * az;
+            dx_ = fma_r(lij, ax, dx_);
+            dy_ = fma_r(lij, ay, dy_);
+            dz_ = fma_r(lij, az, dz_);
             return true;
         });
         R invRest = (p.rest > R(0)) ? (R(1) / p.rest) : R(0);
@@ -369,7 +385,7 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
         if (p.enable_disp_clamp) {
             R maxDisp = p.disp_clamp_max_h * p.h;
             R maxDisp2 = maxDisp * maxDisp;
-            R len2 = ex * ex + ey * ey + ez * ez;
+            R len2 = fma_r(ez, ez, fma_r(ex, ex, ey * ey));
             if (len2 > maxDisp2) {
                 R len = std::sqrt(len2);
                 R sc = maxDisp / (len + R(1e-20f));
@@ -405,14 +421,14 @@ void xsph_t(V4<R>* vel_out, const V4<R>* vel_in, const V4<R>* pred, const uint32
             if (j == i) return true;
             const V4<R> pj = pred[j];
             R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            R r2 = rx * rx + ry * ry + rz * rz;
+            R r2 = fma_r(rz, rz, fma_r(rx, rx, ry * ry));
             if (r2 > p.h2) return true;
             R hr2 = p.h2 - r2;
             R w = p.poly6 * hr2 * hr2 * hr2;
             const V4<R> vj = vel_in[j];
-            sx += (vj.x - vi.x) * w;
-            sy += (vj.y - vi.y) * w;
-            sz += (vj.z - vi.z) * w;
+            sx = fma_r(vj.x - vi.x, w, sx);
+            sy = fma_r(vj.y - vi.y, w, sy);
+            sz = fma_r(vj.z - vi.z, w, sz);
             ++count;
             return true;
         });
@@ -425,7 +441,7 @@ void xsph_t(V4<R>* vel_out, const V4<R>* vel_in, const V4<R>* pred, const uint32
         }
         R mor = (p.rest > R(0)) ? (p.mass / p.rest) : R(0);
         R c = (p.xsph_c * gate) * mor;
-        vel_out[i] = {vi.x + c * sx, vi.y + c * sy, vi.z + c * sz, R(0)};
+        vel_out[i] = {fma_r(c, sx, vi.x), fma_r(c, sy, vi.y), fma_r(c, sz, vi.z), R(0)};
     }
 }
 

@@ -1,11 +1,11 @@
 """The fused GB300 step (pbf_create / pbf_step) vs the CPU oracle step.
 
 Per step, from the same state: sorted keys, permutation and cell tables
-bit-exact; lambda (last iteration), positions and velocities within
-TOL = 1e-5 relative to max(|x|, 1% of max|x|).  Multi-step runs compare each
-step from the GPU's own state (trajectories of this chaotic system are not
-comparable over many steps).  Full-size runs are checked through properties
-that do not depend on size.
+bit-exact; lambda of a single iteration bit-exact; positions, the last
+iteration's lambda and velocities within the bars of tests/parity.py (the
+oracle's powf is the C library's, CUDA's is not correctly rounded).
+Multi-step runs compare each step from the GPU's own state.  Full-size runs
+are checked through properties that do not depend on size.
 """
 import ctypes as C
 
@@ -13,10 +13,9 @@ import numpy as np
 import pytest
 
 import pbfx
+from parity import STEP_LAMBDA, STEP_POS, STEP_VEL, STEP_VEL_FLOOR
 
 pytestmark = pytest.mark.gpu
-
-TOL = 1e-5
 
 
 def c1_scene(lib, iters=2):
@@ -26,6 +25,7 @@ def c1_scene(lib, iters=2):
 
 
 def compare_step(lib, orc, p, pos, vel, hashed, check_lambda=True):
+    iters = p.solverIters
     with pbfx.Sim(lib, p, hashed=hashed) as s:
         s.upload(pos, vel)
         s.step()
@@ -49,9 +49,15 @@ def compare_step(lib, orc, p, pos, vel, hashed, check_lambda=True):
         np.testing.assert_array_equal(st, tr["cell_start"])
         np.testing.assert_array_equal(en, tr["cell_end"])
     if check_lambda:
-        pbfx.assert_close(lam, tr["lambda"], TOL, "lambda")
-    pbfx.assert_close(gpos, opos, TOL, "positions")
-    pbfx.assert_close(gvel, ovel, TOL, "velocities")
+        if iters == 1:
+            np.testing.assert_array_equal(lam, tr["lambda"])  # from the prediction: exact
+        else:
+            pbfx.assert_close(lam, tr["lambda"], STEP_LAMBDA, "lambda")
+    if iters == 0:
+        np.testing.assert_array_equal(gpos, opos)
+        np.testing.assert_array_equal(gvel, ovel)
+    pbfx.assert_close(gpos, opos, STEP_POS, "positions")
+    pbfx.assert_close(gvel, ovel, STEP_VEL, "velocities", floor_frac=STEP_VEL_FLOOR)
     assert np.all(gpos[:, 3] == 1.0) and np.all(gvel[:, 3] == 0.0)
     return gpos, gvel
 
@@ -108,8 +114,8 @@ def test_parameter_change_between_steps(gpu, lib, orc):
         gpos, gvel = s.download()
     opos, ovel = a_pos.copy(), a_vel.copy()
     pbfx.oracle_step(orc, p2, True, opos, ovel, trace=False)
-    pbfx.assert_close(gpos, opos, TOL, "positions")
-    pbfx.assert_close(gvel, ovel, TOL, "velocities")
+    pbfx.assert_close(gpos, opos, STEP_POS, "positions")
+    pbfx.assert_close(gvel, ovel, STEP_VEL, "velocities", floor_frac=STEP_VEL_FLOOR)
 
 
 def test_deterministic(gpu, lib):
