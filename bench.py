@@ -344,9 +344,27 @@ def run_ours(args, cfg, world, rank, local):
                           "unit": "GB/s",
                           "frac": value * step_alg_bytes(nc, cfg["iters"]) / 1e9 / hbm_peak},
         "phase_ms": {k: round(v, 5) for k, v in avg.items()},
+        "step_ms": {"first": round(step_ms[0], 4), "median": round(statistics.median(step_ms), 4),
+                    "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
         "gpu_launches": launches,
         "clocks": clk,
     }
+
+    # The reference's own CUDA kernels (compiled from its sources for sm_103a,
+    # driven in its phase order by oracle/ref/ref_harness.cu, one CUDA graph
+    # per step as sim::Simulator does) over the same step window.
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        ref = pbfx.load_ref()
+        if ref is not None:
+            rpos, rvel = pos.copy(), np.zeros_like(pos)
+            ms = C.c_double()
+            rc = ref.ref_time_steps(pp, 1 if hashed else 0, pbfx.ptr(rpos), pbfx.ptr(rvel), n, args.warmup, args.steps,
+                                    C.byref(ms))
+            if rc == 0:
+                line["reference_gpu"] = {
+                    "value": n / (ms.value * 1e-3), "unit": UNIT, "ms_per_step": ms.value,
+                    "what": "reference kernels (sim/*.cu) built for sm_103a, same steps, graph per step, "
+                            "no L2 flush between steps", "speedup": value / (n / (ms.value * 1e-3))}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = pbfx.load_oracle()
@@ -371,6 +389,7 @@ def main(argv=None):
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU-baseline work")
     ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

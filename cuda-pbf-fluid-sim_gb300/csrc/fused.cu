@@ -22,7 +22,11 @@ namespace pbf {
 namespace {
 
 constexpr int kBS = 256;
+// Neighbour kernels: 128 threads, a 32-entry neighbour queue per thread in
+// shared memory (16 KB per block), column-major so a warp's queue writes hit
+// 32 distinct banks.
 constexpr int kNbrBS = 128;
+constexpr int kQueue = 32;
 
 __global__ void __launch_bounds__(kBS) k_predict_keys(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                       const sim::DeviceParams* __restrict__ dpp, uint32_t N,
@@ -50,15 +54,15 @@ __global__ void __launch_bounds__(kNbrBS) k_lambda(const float4* __restrict__ pr
                                                    const uint32_t* __restrict__ lb,
                                                    const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                    float* __restrict__ lam) {
+    __shared__ uint32_t s_queue[kQueue * kNbrBS];
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= N) return;
+    const bool active = s < N;  // every lane takes part in the warp-wide rounds
+    const uint32_t sc = active ? s : 0u;
     const sim::DeviceParams& dp = *dpp;
     int cx, cy, cz;
-    decode_key(key_s[s], dp.grid.dim, cx, cy, cz);
-    lam[s] = lambda_of(s, pred[s], cx, cy, cz, dp, LbRows{lb}, [&](uint32_t k, uint32_t& j) {
-        j = k;
-        return __ldg(pred + k);
-    });
+    decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+    const float l = lambda_queued<kQueue, kNbrBS>(active, sc, pred[sc], cx, cy, cz, dp, lb, pred, s_queue + threadIdx.x);
+    if (active) lam[s] = l;
 }
 
 template <bool kLast>
@@ -67,28 +71,28 @@ __global__ void __launch_bounds__(kNbrBS) k_delta(const float4* __restrict__ pre
                                                   const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                   float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
                                                   float4* __restrict__ vel_s) {
+    __shared__ uint32_t s_queue[kQueue * kNbrBS];
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= N) return;
+    const bool active = s < N;  // every lane takes part in the warp-wide rounds
+    const uint32_t sc = active ? s : 0u;
     const sim::DeviceParams& dp = *dpp;
     int cx, cy, cz;
-    decode_key(key_s[s], dp.grid.dim, cx, cy, cz);
-    const float4 pi = pred[s];
-    const float3 d = delta_of(s, pi, lam[s], cx, cy, cz, dp, scorr_wq(dp), LbRows{lb},
-                              [&](uint32_t k, uint32_t& j, float& lj) {
-                                  j = k;
-                                  lj = __ldg(lam + k);
-                                  return __ldg(pred + k);
-                              });
-    float4 x = make_float4(pi.x + d.x, pi.y + d.y, pi.z + d.z, pi.w);
+    decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+    const float4 pi = pred[sc];
+    const float3 d = delta_queued<kQueue, kNbrBS>(active, sc, pi, lam[sc], cx, cy, cz, dp, scorr_wq(dp), lb, pred,
+                                                   lam, s_queue + threadIdx.x);
+    if (!active) return;
+    float4 x = make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w);
     if (kLast) {
         // Boundary(e=0) after the solve loop (sim/phases.cpp:94); its velocity
         // half is overwritten by the velocity phase, so only x is clamped.
         float4 vdummy = make_float4(0.f, 0.f, 0.f, 0.f);
         boundary_apply(x, vdummy, dp.grid, 0.0f);
         // PhaseVelocity (sim/phases.cpp:102-105): v = (x - p) * (1/dt).
-        const float inv_dt = 1.0f / dp.dt;
+        const float inv_dt = div_(1.0f, dp.dt);
         const float4 p = pos_s[s];
-        vel_s[s] = make_float4((x.x - p.x) * inv_dt, (x.y - p.y) * inv_dt, (x.z - p.z) * inv_dt, 0.0f);
+        vel_s[s] = make_float4(mul_(sub_(x.x, p.x), inv_dt), mul_(sub_(x.y, p.y), inv_dt),
+                               mul_(sub_(x.z, p.z), inv_dt), 0.0f);
     }
     pred_out[s] = x;
 }
@@ -102,9 +106,10 @@ __global__ void __launch_bounds__(kBS) k_finalize_no_iters(float4* __restrict__ 
     float4 x = pred[s];
     float4 vdummy = make_float4(0.f, 0.f, 0.f, 0.f);
     boundary_apply(x, vdummy, dpp->grid, 0.0f);
-    const float inv_dt = 1.0f / dpp->dt;
+    const float inv_dt = div_(1.0f, dpp->dt);
     const float4 p = pos_s[s];
-    vel_s[s] = make_float4((x.x - p.x) * inv_dt, (x.y - p.y) * inv_dt, (x.z - p.z) * inv_dt, 0.0f);
+    vel_s[s] = make_float4(mul_(sub_(x.x, p.x), inv_dt), mul_(sub_(x.y, p.y), inv_dt), mul_(sub_(x.z, p.z), inv_dt),
+                           0.0f);
     pred[s] = x;
 }
 
@@ -114,20 +119,19 @@ __global__ void __launch_bounds__(kNbrBS) k_commit(const float4* __restrict__ pr
                                                    const uint32_t* __restrict__ perm,
                                                    const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                    float4* __restrict__ pos, float4* __restrict__ vel) {
+    __shared__ uint32_t s_queue[kXsph ? kQueue * kNbrBS : 1];
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= N) return;
+    const bool active = s < N;  // every lane takes part in the warp-wide rounds
+    const uint32_t sc = active ? s : 0u;
     const sim::DeviceParams& dp = *dpp;
-    float4 x = pred[s];
-    float4 v = vel_s[s];
+    float4 x = pred[sc];
+    float4 v = vel_s[sc];
     if (kXsph && dp.xsph_c > 0.f) {
         int cx, cy, cz;
-        decode_key(key_s[s], dp.grid.dim, cx, cy, cz);
-        v = xsph_of(s, x, v, cx, cy, cz, dp, LbRows{lb}, [&](uint32_t k, uint32_t& j, float4& vj) {
-            j = k;
-            vj = __ldg(vel_s + k);
-            return __ldg(pred + k);
-        });
+        decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+        v = xsph_queued<kQueue, kNbrBS>(active, sc, x, v, cx, cy, cz, dp, lb, pred, vel_s, s_queue + threadIdx.x);
     }
+    if (!active) return;
     boundary_apply(x, v, dp.grid, dp.boundaryRestitution);
     const uint32_t i = perm[s];
     pos[i] = x;

@@ -43,6 +43,24 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// ------------------------------------------------ explicitly rounded math
+// The reference's kernels are compiled with nvcc's default FMA contraction,
+// which fuses some of their multiply-adds.  Which ones depends on the
+// surrounding code, so the neighbour arithmetic here spells every operation
+// out with round-to-nearest intrinsics (never contracted or reassociated) in
+// the reference kernels' fused form: identical results whatever the loop
+// structure around them.  The fused form was identified against the
+// reference kernels' outputs (every lambda and XSPH velocity of 32,768
+// particles bit-identical, lattice and compressed states).
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float div_(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float sqrt_(float a) { return __fsqrt_rn(a); }
+// a*a + b*b + c*c as the reference's (x*x + y*y + z*z) is fused.
+__device__ __forceinline__ float sumsq_(float a, float b, float c) { return fma_(c, c, fma_(a, a, mul_(b, b))); }
+
 // Status word of a decoupled look-back: 2-bit flag | 30-bit count.
 constexpr uint32_t kFlagAggregate = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
@@ -99,12 +117,12 @@ __device__ __forceinline__ float4 predict_clamped(float4 p, float4 v, float3 g, 
 // Full KBoundary on a (position, velocity) pair (sim/boundary.cu:11-25).
 __device__ __forceinline__ void boundary_apply(float4& p, float4& v, const sim::GridBounds& gb, float restitution) {
     const float e = fminf(fmaxf(restitution, 0.0f), 1.0f);
-    if (p.x < gb.mins.x) { p.x = gb.mins.x; v.x *= -e; }
-    if (p.y < gb.mins.y) { p.y = gb.mins.y; v.y *= -e; }
-    if (p.z < gb.mins.z) { p.z = gb.mins.z; v.z *= -e; }
-    if (p.x > gb.maxs.x) { p.x = gb.maxs.x; v.x *= -e; }
-    if (p.y > gb.maxs.y) { p.y = gb.maxs.y; v.y *= -e; }
-    if (p.z > gb.maxs.z) { p.z = gb.maxs.z; v.z *= -e; }
+    if (p.x < gb.mins.x) { p.x = gb.mins.x; v.x = mul_(v.x, -e); }
+    if (p.y < gb.mins.y) { p.y = gb.mins.y; v.y = mul_(v.y, -e); }
+    if (p.z < gb.mins.z) { p.z = gb.mins.z; v.z = mul_(v.z, -e); }
+    if (p.x > gb.maxs.x) { p.x = gb.maxs.x; v.x = mul_(v.x, -e); }
+    if (p.y > gb.maxs.y) { p.y = gb.maxs.y; v.y = mul_(v.y, -e); }
+    if (p.z > gb.maxs.z) { p.z = gb.maxs.z; v.z = mul_(v.z, -e); }
     p.w = 1.0f;
     v.w = 0.0f;
 }
@@ -156,6 +174,78 @@ __device__ __forceinline__ void walk_neighbours(int cx, int cy, int cz, int reac
     }
 }
 
+// Two-phase walk of the same candidates in the same order.  All lanes of a
+// warp scan in lockstep, one candidate per lane per iteration, testing it
+// with hit(k) (cheap) and queueing hits in shared memory (q[j * kStride]).
+// Lanes of one cell share their slot ranges, so in lockstep they load the
+// same candidates (broadcast) and reach row ends together.  When any lane's
+// queue might overflow within the next kChunk candidates, the whole warp
+// drains its queues, running body(k) in order; the expensive body thus runs
+// only for actual neighbours and with most lanes busy.  At most maxHits
+// neighbours are processed (the lambda cap: the reference stops at the first
+// `cap` neighbours in walk order).  Every lane of the warp must call this
+// (inactive lanes with active = false).
+template <int Q, int kStride, class RowRange, class Hit, class Body>
+__device__ __forceinline__ void walk_queued(bool active, int cx, int cy, int cz, int reach, int3 dim,
+                                            RowRange&& rowRange, uint32_t* q, int maxHits, Hit&& hit,
+                                            Body&& body) {
+    constexpr int kChunk = 8;
+    static_assert(Q > kChunk, "queue must hold more than one chunk");
+    const int side = 2 * reach + 1;
+    const int nrows = side * side;
+    const int x0 = max(cx - reach, 0);
+    const int x1 = min(cx + reach, dim.x - 1);
+    int ri = -1, total = 0, cnt = 0;
+    uint32_t k = 0, e = 0;
+    bool done = !active;
+    // next in-bounds (dz, dy) row, dz outer, with a non-empty slot range
+    auto next_row = [&]() {
+        for (;;) {
+            if (++ri >= nrows) {
+                done = true;
+                return;
+            }
+            const int z = cz + ri / side - reach;
+            const int y = cy + ri % side - reach;
+            if (z < 0 || z >= dim.z || y < 0 || y >= dim.y) continue;
+            const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
+            const uint2 r = rowRange(row + uint32_t(x0), row + uint32_t(x1));
+            k = r.x;
+            e = r.y;
+            if (k < e) return;
+        }
+    };
+    if (!done) next_row();
+    for (;;) {
+        const bool any = __any_sync(0xFFFFFFFFu, !done);
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u) {
+            if (!done) {
+                if (hit(k)) {
+                    q[cnt * kStride] = k;
+                    ++cnt;
+                    if (++total >= maxHits) done = true;
+                }
+                if (!done && ++k >= e) next_row();
+            }
+        }
+        if (!any || __any_sync(0xFFFFFFFFu, cnt > Q - kChunk)) {
+            for (int j = 0; j < cnt; ++j) body(q[j * kStride]);
+            cnt = 0;
+            if (!any) break;
+        }
+    }
+}
+
+// r^2 of a candidate as the reference's neighbour loops compute it
+// (sim/pbf_lambda.cu:67-68).
+__device__ __forceinline__ float dist2(float4 pi, float4 pj, float& rx, float& ry, float& rz) {
+    rx = sub_(pi.x, pj.x);
+    ry = sub_(pi.y, pj.y);
+    rz = sub_(pi.z, pj.z);
+    return sumsq_(rx, ry, rz);
+}
+
 // Row ranges from a dense lower-bound table lb[c] = first sorted slot whose
 // key >= c (numCells+1 entries).
 struct LbRows {
@@ -205,47 +295,43 @@ struct CompactRows {
 };
 
 // ---------------------------------------------------------------- lambda
-// Per-particle constraint multiplier, sim/pbf_lambda.cu:38-107.  fetch(k)
-// returns the candidate's identity (compared with `self`) and position.
-template <class RowRange, class Fetch>
-__device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int cy, int cz,
-                                           const sim::DeviceParams& dp, RowRange&& rows, Fetch&& fetch) {
-    const sim::KernelCoeffs& kc = dp.kernel;
-    const sim::PbfTuning& pbf = dp.pbf;
-    const float particleMass = dp.particleMass;
-    const float restDensity = dp.restDensity;
+// Per-particle constraint multiplier, sim/pbf_lambda.cu:38-107, split into a
+// per-neighbour accumulation and a finaliser (the expressions are the
+// reference's, evaluated in its order).
+struct LambdaAcc {
     float density = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, sumGrad2 = 0.f;
     int contrib = 0;
-    const int cap = dp.maxNeighbors;
-    const bool hasCap = cap > 0;
-    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
-        if (hasCap && contrib >= cap) return false;
-        uint32_t j;
-        const float4 pj = fetch(k, j);
-        if (j == self) return true;
-        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 > kc.h2) return true;
-        ++contrib;
-        const float hr2 = kc.h2 - r2;
-        density += particleMass * kc.poly6 * hr2 * hr2 * hr2;
-        const float r = sqrtf(r2);
-        const float r_safe = fmaxf(r, pbf.grad_r_eps);
-        const float t = kc.h - r;
-        const float coeff = (-3.0f * kc.spiky * (t * t) / r_safe);
-        const float ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
-        gx += ax; gy += ay; gz += az;
-        sumGrad2 += ax * ax + ay * ay + az * az;
-        return true;
-    });
-    const float gradSum2 = gx * gx + gy * gy + gz * gz;
-    const float scale = (restDensity > 0.f) ? (particleMass / restDensity) : 0.f;
-    float denom = (scale * scale) * (sumGrad2 + gradSum2) + pbf.lambda_denom_eps;
-    if (pbf.compliance > 0.f && dp.dt > 0.f) denom += pbf.compliance / (dp.dt * dp.dt);
+};
+
+__device__ __forceinline__ void lambda_accumulate(LambdaAcc& a, float rx, float ry, float rz, float r2,
+                                                  const sim::DeviceParams& dp) {
+    const sim::KernelCoeffs& kc = dp.kernel;
+    ++a.contrib;
+    const float hr2 = sub_(kc.h2, r2);
+    a.density = fma_(mul_(mul_(mul_(dp.particleMass, kc.poly6), hr2), hr2), hr2, a.density);
+    const float r = sqrt_(r2);
+    const float r_safe = fmaxf(r, dp.pbf.grad_r_eps);
+    const float t = sub_(kc.h, r);
+    const float coeff = div_(mul_(mul_(-3.0f, kc.spiky), mul_(t, t)), r_safe);
+    const float ax = mul_(coeff, rx), ay = mul_(coeff, ry), az = mul_(coeff, rz);
+    a.gx = add_(a.gx, ax);
+    a.gy = add_(a.gy, ay);
+    a.gz = add_(a.gz, az);
+    a.sumGrad2 = add_(a.sumGrad2, sumsq_(ax, ay, az));
+}
+
+__device__ __forceinline__ float lambda_finalize(const LambdaAcc& a, const sim::DeviceParams& dp) {
+    const sim::PbfTuning& pbf = dp.pbf;
+    const float restDensity = dp.restDensity;
+    const float gradSum2 = sumsq_(a.gx, a.gy, a.gz);
+    const float scale = (restDensity > 0.f) ? div_(dp.particleMass, restDensity) : 0.f;
+    const float sum = add_(a.sumGrad2, gradSum2);
+    float denom = fma_(mul_(scale, scale), sum, pbf.lambda_denom_eps);
+    if (pbf.compliance > 0.f && dp.dt > 0.f) denom = add_(denom, div_(pbf.compliance, mul_(dp.dt, dp.dt)));
     denom = fmaxf(denom, pbf.lambda_denom_eps);
-    if (contrib < 2 || (sumGrad2 + gradSum2) < 1e-12f) return 0.0f;
-    const float C = (restDensity > 0.f) ? (density / restDensity - 1.f) : 0.f;
-    float lam = -C / denom;
+    if (a.contrib < 2 || sum < 1e-12f) return 0.0f;
+    const float C = (restDensity > 0.f) ? sub_(div_(a.density, restDensity), 1.f) : 0.f;
+    float lam = div_(-C, denom);
     if (!isfinite(lam)) lam = 0.f;
     if (pbf.enable_lambda_clamp) {
         if (fabsf(lam) > pbf.lambda_max_abs) lam = copysignf(pbf.lambda_max_abs, lam);
@@ -253,107 +339,216 @@ __device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int
     return lam;
 }
 
+// Single-pass walk (reference layout): fetch(k, j) returns the candidate's
+// position and writes its identity j (compared with `self`).
+template <class RowRange, class Fetch>
+__device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int cy, int cz,
+                                           const sim::DeviceParams& dp, RowRange&& rows, Fetch&& fetch) {
+    LambdaAcc a;
+    const int cap = dp.maxNeighbors;
+    const bool hasCap = cap > 0;
+    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
+        if (hasCap && a.contrib >= cap) return false;
+        uint32_t j;
+        const float4 pj = fetch(k, j);
+        if (j == self) return true;
+        float rx, ry, rz;
+        const float r2 = dist2(pi, pj, rx, ry, rz);
+        if (r2 > dp.kernel.h2) return true;
+        lambda_accumulate(a, rx, ry, rz, r2, dp);
+        return true;
+    });
+    return lambda_finalize(a, dp);
+}
+
+// Two-phase walk over cell-ordered positions (slot k is particle k).
+template <int Q, int kStride>
+__device__ __forceinline__ float lambda_queued(bool active, uint32_t s, float4 pi, int cx, int cy, int cz,
+                                               const sim::DeviceParams& dp, const uint32_t* __restrict__ lb,
+                                               const float4* __restrict__ pred, uint32_t* q) {
+    LambdaAcc a;
+    const int cap = dp.maxNeighbors;
+    const float h2 = dp.kernel.h2;
+    walk_queued<Q, kStride>(
+        active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, q, cap > 0 ? cap : 0x7FFFFFFF,
+        [&](uint32_t k) -> bool {
+            float rx, ry, rz;
+            return k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > h2);
+        },
+        [&](uint32_t k) {
+            float rx, ry, rz;
+            const float r2 = dist2(pi, __ldg(pred + k), rx, ry, rz);
+            lambda_accumulate(a, rx, ry, rz, r2, dp);
+        });
+    return lambda_finalize(a, dp);
+}
+
 // s_corr exponent: powf, as the reference (sim/pbf_delta_apply.cu:82).
 __device__ __forceinline__ float scorr_pow(float ratio, float n) { return powf(ratio, n); }
 
 // w_q of the tensile-instability term (sim/pbf_delta_apply.cu:40-42).
 __device__ __forceinline__ float scorr_wq(const sim::DeviceParams& dp) {
-    const float dq = dp.pbf.scorr_dq_h * dp.kernel.h;
-    const float hr2_q = dp.kernel.h2 - dq * dq;
-    return (hr2_q > 0.f) ? (dp.kernel.poly6 * hr2_q * hr2_q * hr2_q) : dp.pbf.wq_min;
+    const float dq = mul_(dp.pbf.scorr_dq_h, dp.kernel.h);
+    const float hr2_q = fma_(-dq, dq, dp.kernel.h2);
+    return (hr2_q > 0.f) ? mul_(mul_(mul_(dp.kernel.poly6, hr2_q), hr2_q), hr2_q) : dp.pbf.wq_min;
 }
 
 // ----------------------------------------------------------------- delta
-// Position correction, sim/pbf_delta_apply.cu:40-112.  fetch(k, j, lam_j)
-// returns the candidate position and writes its identity and lambda.
-template <class RowRange, class Fetch>
-__device__ __forceinline__ float3 delta_of(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
-                                           const sim::DeviceParams& dp, float w_q, RowRange&& rows, Fetch&& fetch) {
+// Position correction, sim/pbf_delta_apply.cu:40-112.
+__device__ __forceinline__ void delta_accumulate(float3& d, float rx, float ry, float rz, float r2, float lam_i,
+                                                 float lam_j, float w_q, const sim::DeviceParams& dp) {
     const sim::KernelCoeffs& kc = dp.kernel;
     const sim::PbfTuning& pbf = dp.pbf;
-    float dx = 0.f, dy = 0.f, dz = 0.f;
-    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
-        uint32_t j;
-        float lam_j;
-        const float4 pj = fetch(k, j, lam_j);
-        if (j == self) return true;
-        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 > kc.h2) return true;
-        const float r = sqrtf(r2);
-        const float t = kc.h - r;
-        const float r_safe = fmaxf(r, pbf.grad_r_eps);
-        const float coeff = (-3.0f * kc.spiky * (t * t) / r_safe);
-        const float ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
-        float scorr = 0.0f;
-        if (pbf.scorr_enable) {
-            const float hr2 = kc.h2 - r2;
-            const float w = kc.poly6 * hr2 * hr2 * hr2;
-            const float ratio = (w_q > 0.f) ? (w / w_q) : 0.0f;
-            scorr = -pbf.scorr_k * scorr_pow(ratio, pbf.scorr_n);
-            if (pbf.scorr_min < 0.f) scorr = fmaxf(scorr, pbf.scorr_min);
-        }
-        const float lij = (lam_i + lam_j + scorr);
-        dx += lij * ax;
-        dy += lij * ay;
-        dz += lij * az;
-        return true;
-    });
-    const float invRest = (dp.restDensity > 0.f) ? (1.0f / dp.restDensity) : 0.f;
-    float3 d = make_float3(invRest * dx, invRest * dy, invRest * dz);
+    const float r = sqrt_(r2);
+    const float t = sub_(kc.h, r);
+    const float r_safe = fmaxf(r, pbf.grad_r_eps);
+    const float coeff = div_(mul_(mul_(-3.0f, kc.spiky), mul_(t, t)), r_safe);
+    const float ax = mul_(coeff, rx), ay = mul_(coeff, ry), az = mul_(coeff, rz);
+    float scorr = 0.0f;
+    if (pbf.scorr_enable) {
+        const float hr2 = sub_(kc.h2, r2);
+        const float w = mul_(mul_(mul_(kc.poly6, hr2), hr2), hr2);
+        const float ratio = (w_q > 0.f) ? div_(w, w_q) : 0.0f;
+        scorr = mul_(-pbf.scorr_k, scorr_pow(ratio, pbf.scorr_n));
+        if (pbf.scorr_min < 0.f) scorr = fmaxf(scorr, pbf.scorr_min);
+    }
+    const float lij = add_(add_(lam_i, lam_j), scorr);
+    d.x = fma_(lij, ax, d.x);
+    d.y = fma_(lij, ay, d.y);
+    d.z = fma_(lij, az, d.z);
+}
+
+__device__ __forceinline__ float3 delta_finalize(float3 dsum, const sim::DeviceParams& dp) {
+    const sim::PbfTuning& pbf = dp.pbf;
+    const float invRest = (dp.restDensity > 0.f) ? div_(1.0f, dp.restDensity) : 0.f;
+    float3 d = make_float3(mul_(invRest, dsum.x), mul_(invRest, dsum.y), mul_(invRest, dsum.z));
     if (pbf.enable_relax) {
-        d.x *= pbf.relax_omega;
-        d.y *= pbf.relax_omega;
-        d.z *= pbf.relax_omega;
+        d.x = mul_(d.x, pbf.relax_omega);
+        d.y = mul_(d.y, pbf.relax_omega);
+        d.z = mul_(d.z, pbf.relax_omega);
     }
     if (pbf.enable_disp_clamp) {
-        const float maxDisp = pbf.disp_clamp_max_h * kc.h;
-        const float maxDisp2 = maxDisp * maxDisp;
-        const float len2 = d.x * d.x + d.y * d.y + d.z * d.z;
+        const float maxDisp = mul_(pbf.disp_clamp_max_h, dp.kernel.h);
+        const float maxDisp2 = mul_(maxDisp, maxDisp);
+        const float len2 = sumsq_(d.x, d.y, d.z);
         if (len2 > maxDisp2) {
-            const float len = sqrtf(len2);
-            const float s = maxDisp / (len + 1e-20f);
-            d.x *= s; d.y *= s; d.z *= s;
+            const float len = sqrt_(len2);
+            const float s = div_(maxDisp, add_(len, 1e-20f));
+            d.x = mul_(d.x, s);
+            d.y = mul_(d.y, s);
+            d.z = mul_(d.z, s);
         }
     }
     return d;
 }
 
+// fetch(k, j, lam_j) returns the candidate position and writes its identity
+// and lambda.
+template <class RowRange, class Fetch>
+__device__ __forceinline__ float3 delta_of(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
+                                           const sim::DeviceParams& dp, float w_q, RowRange&& rows, Fetch&& fetch) {
+    float3 dsum = make_float3(0.f, 0.f, 0.f);
+    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
+        uint32_t j;
+        float lam_j;
+        const float4 pj = fetch(k, j, lam_j);
+        if (j == self) return true;
+        float rx, ry, rz;
+        const float r2 = dist2(pi, pj, rx, ry, rz);
+        if (r2 > dp.kernel.h2) return true;
+        delta_accumulate(dsum, rx, ry, rz, r2, lam_i, lam_j, w_q, dp);
+        return true;
+    });
+    return delta_finalize(dsum, dp);
+}
+
+template <int Q, int kStride>
+__device__ __forceinline__ float3 delta_queued(bool active, uint32_t s, float4 pi, float lam_i, int cx, int cy, int cz,
+                                               const sim::DeviceParams& dp, float w_q,
+                                               const uint32_t* __restrict__ lb, const float4* __restrict__ pred,
+                                               const float* __restrict__ lam, uint32_t* q) {
+    float3 dsum = make_float3(0.f, 0.f, 0.f);
+    const float h2 = dp.kernel.h2;
+    walk_queued<Q, kStride>(
+        active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, q, 0x7FFFFFFF,
+        [&](uint32_t k) -> bool {
+            float rx, ry, rz;
+            return k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > h2);
+        },
+        [&](uint32_t k) {
+            float rx, ry, rz;
+            const float r2 = dist2(pi, __ldg(pred + k), rx, ry, rz);
+            delta_accumulate(dsum, rx, ry, rz, r2, lam_i, __ldg(lam + k), w_q, dp);
+        });
+    return delta_finalize(dsum, dp);
+}
+
 // ------------------------------------------------------------------ xsph
-// Jacobi XSPH, sim/xsph.cu:39-95.  fetch(k, j, vj) returns the candidate
-// position and writes its identity and (old) velocity.
+// Jacobi XSPH, sim/xsph.cu:39-95.
+__device__ __forceinline__ void xsph_accumulate(float3& sum, int& count, float r2, float4 vi, float4 vj,
+                                                const sim::DeviceParams& dp) {
+    const float hr2 = sub_(dp.kernel.h2, r2);
+    const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
+    sum.x = fma_(sub_(vj.x, vi.x), w, sum.x);
+    sum.y = fma_(sub_(vj.y, vi.y), w, sum.y);
+    sum.z = fma_(sub_(vj.z, vi.z), w, sum.z);
+    ++count;
+}
+
+__device__ __forceinline__ float4 xsph_finalize(float3 sum, int count, float4 vi, const sim::DeviceParams& dp) {
+    float gate = 1.0f;
+    if (dp.pbf.xsph_gate_enable) {
+        const int nMin = max(0, dp.pbf.xsph_n_min);
+        const int nMax = max(nMin + 1, dp.pbf.xsph_n_max);
+        const float t = div_(sub_(float(count), float(nMin)), float(nMax - nMin));
+        gate = fminf(1.f, fmaxf(0.f, t));
+    }
+    const float mor = (dp.restDensity > 0.f) ? div_(dp.particleMass, dp.restDensity) : 0.f;
+    const float c = mul_(mul_(dp.xsph_c, gate), mor);
+    return make_float4(fma_(c, sum.x, vi.x), fma_(c, sum.y, vi.y), fma_(c, sum.z, vi.z), 0.0f);
+}
+
+// fetch(k, j, vj) returns the candidate position and writes its identity
+// and (old) velocity.
 template <class RowRange, class Fetch>
 __device__ __forceinline__ float4 xsph_of(uint32_t self, float4 pi, float4 vi, int cx, int cy, int cz,
                                           const sim::DeviceParams& dp, RowRange&& rows, Fetch&& fetch) {
-    const sim::KernelCoeffs& kc = dp.kernel;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
+    float3 sum = make_float3(0.f, 0.f, 0.f);
     int count = 0;
     walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
         uint32_t j;
         float4 vj;
         const float4 pj = fetch(k, j, vj);
         if (j == self) return true;
-        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 > kc.h2) return true;
-        const float hr2 = kc.h2 - r2;
-        const float w = kc.poly6 * hr2 * hr2 * hr2;
-        sx += (vj.x - vi.x) * w;
-        sy += (vj.y - vi.y) * w;
-        sz += (vj.z - vi.z) * w;
-        ++count;
+        float rx, ry, rz;
+        const float r2 = dist2(pi, pj, rx, ry, rz);
+        if (r2 > dp.kernel.h2) return true;
+        xsph_accumulate(sum, count, r2, vi, vj, dp);
         return true;
     });
-    float gate = 1.0f;
-    if (dp.pbf.xsph_gate_enable) {
-        const int nMin = max(0, dp.pbf.xsph_n_min);
-        const int nMax = max(nMin + 1, dp.pbf.xsph_n_max);
-        const float t = (float(count) - float(nMin)) / float(nMax - nMin);
-        gate = fminf(1.f, fmaxf(0.f, t));
-    }
-    const float mor = (dp.restDensity > 0.f) ? (dp.particleMass / dp.restDensity) : 0.f;
-    return make_float4(vi.x + (dp.xsph_c * gate) * mor * sx, vi.y + (dp.xsph_c * gate) * mor * sy,
-                       vi.z + (dp.xsph_c * gate) * mor * sz, 0.0f);
+    return xsph_finalize(sum, count, vi, dp);
+}
+
+template <int Q, int kStride>
+__device__ __forceinline__ float4 xsph_queued(bool active, uint32_t s, float4 pi, float4 vi, int cx, int cy, int cz,
+                                              const sim::DeviceParams& dp, const uint32_t* __restrict__ lb,
+                                              const float4* __restrict__ pred, const float4* __restrict__ vel,
+                                              uint32_t* q) {
+    float3 sum = make_float3(0.f, 0.f, 0.f);
+    int count = 0;
+    const float h2 = dp.kernel.h2;
+    walk_queued<Q, kStride>(
+        active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, q, 0x7FFFFFFF,
+        [&](uint32_t k) -> bool {
+            float rx, ry, rz;
+            return k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > h2);
+        },
+        [&](uint32_t k) {
+            float rx, ry, rz;
+            const float r2 = dist2(pi, __ldg(pred + k), rx, ry, rz);
+            xsph_accumulate(sum, count, r2, vi, __ldg(vel + k), dp);
+        });
+    return xsph_finalize(sum, count, vi, dp);
 }
 
 // Grid size helper.

@@ -377,8 +377,9 @@ int Simulator::launchesPerStep() const {
 }
 
 int Simulator::profileStep(const SimParams& p, float* ms, const char** names, int cap) {
-    // Bring buffers/params up to date exactly like step(), then run the
-    // phases eagerly with events between them.
+    // Bring buffers/params up to date exactly like step(), then capture the
+    // phases with external event-record nodes between them into one graph:
+    // the events time the device work only (no host enqueue gaps).
     SimParams np = p;
     np.grid.dim = compute_dims(p.grid);
     const uint32_t nc = num_cells(np.grid.dim);
@@ -395,10 +396,12 @@ int Simulator::profileStep(const SimParams& p, float* ms, const char** names, in
     auto mark = [&](const char* name) {
         cudaEvent_t e;
         cudaEventCreate(&e);
-        cudaEventRecord(e, m_stream);
+        cudaEventRecordWithFlags(e, m_stream, cudaEventRecordExternal);
         ev.push_back(e);
         if (name) nm.push_back(name);
     };
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1;
     mark(nullptr);
     pbf::fused_predict_keys(b, sh, m_stream);
     mark("predict_keys");
@@ -422,13 +425,22 @@ int Simulator::profileStep(const SimParams& p, float* ms, const char** names, in
     }
     pbf::fused_commit(b, sh, m_stream);
     mark("commit");
-    cudaStreamSynchronize(m_stream);
     int n = 0;
-    for (size_t k = 1; k < ev.size() && n < cap; ++k, ++n) {
-        cudaEventElapsedTime(&ms[n], ev[k - 1], ev[k]);
-        if (names) names[n] = nm[k - 1];
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamEndCapture(m_stream, &graph) == cudaSuccess && graph &&
+        cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess && cudaGraphLaunch(exec, m_stream) == cudaSuccess &&
+        cudaStreamSynchronize(m_stream) == cudaSuccess) {
+        for (size_t k = 1; k < ev.size() && n < cap; ++k, ++n) {
+            if (cudaEventElapsedTime(&ms[n], ev[k - 1], ev[k]) != cudaSuccess) ms[n] = -1.f;
+            if (names) names[n] = nm[k - 1];
+        }
+    } else {
+        n = -1;
     }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    cudaGetLastError();
     return n;
 }
 

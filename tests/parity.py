@@ -15,16 +15,25 @@ GPU vs the CPU oracle:
     s_corr exponent is the C library's powf, CUDA's powf is not correctly
     rounded, so a few terms differ by an ulp;
   * state after a full step: STEP_POS for positions (they differ by at most
-    1-2 ulps); STEP_VEL for velocities, normwise: v = (x - p) / dt turns a
-    position ulp into 1/dt = 120 ulps of an O(1) quantity, so slow particles
-    are compared against the velocity scale; STEP_LAMBDA for the last
-    iteration's lambda, because the ulps pass through the next solver
-    iteration of the reference's ill-conditioned displacement step (a sum of
-    large cancelling terms that is then clamped to 0.05 h).
+    1-2 ulps); velocities through the displacement they encode,
+    |v_a - v_b| * dt <= STEP_POS * max|x| (v = (x - p) / dt turns one
+    position ulp into 1/dt = 120 ulps of velocity); the last iteration's
+    lambda normwise (floor = max|lambda|) at STEP_LAMBDA, because those ulps
+    pass through the next solver iteration of the reference's ill-conditioned
+    displacement step (a sum of large cancelling terms that is then clamped
+    to 0.05 h) and lambda = -C/denom with C = rho/rho0 - 1 near zero for many
+    particles.
 """
+import numpy as np
 
 PHASE_DELTA = 1e-5  # normwise (floor = max|b|)
 STEP_POS = 1e-5
-STEP_VEL = 1e-5  # normwise (floor = max|b|)
-STEP_VEL_FLOOR = 1.0
-STEP_LAMBDA = 1e-4
+STEP_LAMBDA = 1e-5  # normwise (floor = max|b|)
+STEP_LAMBDA_FLOOR = 1.0
+
+
+def assert_velocities_close(v_a, v_b, pos_b, dt):
+    err = float(np.max(np.abs(np.float64(v_a[:, :3]) - np.float64(v_b[:, :3])))) * float(dt)
+    scale = float(np.max(np.abs(pos_b[:, :3])))
+    if not err <= STEP_POS * scale:
+        raise AssertionError("velocities: |dv|*dt = %.3e > %.1e * max|x| (%.3e)" % (err, STEP_POS, STEP_POS * scale))

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import pbfx
-from parity import STEP_LAMBDA, STEP_POS, STEP_VEL, STEP_VEL_FLOOR
+from parity import STEP_LAMBDA, STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close
 
 pytestmark = pytest.mark.gpu
 
@@ -52,12 +52,12 @@ def compare_step(lib, orc, p, pos, vel, hashed, check_lambda=True):
         if iters == 1:
             np.testing.assert_array_equal(lam, tr["lambda"])  # from the prediction: exact
         else:
-            pbfx.assert_close(lam, tr["lambda"], STEP_LAMBDA, "lambda")
+            pbfx.assert_close(lam, tr["lambda"], STEP_LAMBDA, "lambda", floor_frac=STEP_LAMBDA_FLOOR)
     if iters == 0:
         np.testing.assert_array_equal(gpos, opos)
         np.testing.assert_array_equal(gvel, ovel)
     pbfx.assert_close(gpos, opos, STEP_POS, "positions")
-    pbfx.assert_close(gvel, ovel, STEP_VEL, "velocities", floor_frac=STEP_VEL_FLOOR)
+    assert_velocities_close(gvel, ovel, opos, p.dt)
     assert np.all(gpos[:, 3] == 1.0) and np.all(gvel[:, 3] == 0.0)
     return gpos, gvel
 
@@ -115,7 +115,7 @@ def test_parameter_change_between_steps(gpu, lib, orc):
     opos, ovel = a_pos.copy(), a_vel.copy()
     pbfx.oracle_step(orc, p2, True, opos, ovel, trace=False)
     pbfx.assert_close(gpos, opos, STEP_POS, "positions")
-    pbfx.assert_close(gvel, ovel, STEP_VEL, "velocities", floor_frac=STEP_VEL_FLOOR)
+    assert_velocities_close(gvel, ovel, opos, p2.dt)
 
 
 def test_deterministic(gpu, lib):

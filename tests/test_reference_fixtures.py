@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 import pbfx
-from parity import STEP_LAMBDA, STEP_POS, STEP_VEL, STEP_VEL_FLOOR
+from parity import STEP_LAMBDA, STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
@@ -31,7 +31,7 @@ def load_fixture(path):
     return p, bool(int(z["hashed"])), z
 
 
-def check_against(z, hashed, out_pos, out_vel, tr, exact):
+def check_against(z, hashed, out_pos, out_vel, tr, exact, dt):
     np.testing.assert_array_equal(tr["keys_sorted"], z["keys_sorted"])
     np.testing.assert_array_equal(tr["perm"], z["perm"])
     if hashed:
@@ -46,8 +46,8 @@ def check_against(z, hashed, out_pos, out_vel, tr, exact):
         np.testing.assert_array_equal(out_vel, z["vel_out"])
     else:
         pbfx.assert_close(out_pos, z["pos_out"], STEP_POS, "positions")
-        pbfx.assert_close(tr["lambda"], z["lambda"], STEP_LAMBDA, "lambda")
-        pbfx.assert_close(out_vel, z["vel_out"], STEP_VEL, "velocities", floor_frac=STEP_VEL_FLOOR)
+        pbfx.assert_close(tr["lambda"], z["lambda"], STEP_LAMBDA, "lambda", floor_frac=STEP_LAMBDA_FLOOR)
+        assert_velocities_close(out_vel, z["vel_out"], z["pos_out"], dt)
 
 
 def test_fixtures_present():
@@ -59,7 +59,7 @@ def test_oracle_reproduces_reference(orc, path):
     p, hashed, z = load_fixture(path)
     pos, vel = z["pos_in"].copy(), z["vel_in"].copy()
     tr = pbfx.oracle_step(orc, p, hashed, pos, vel)
-    check_against(z, hashed, pos, vel, tr, exact=False)
+    check_against(z, hashed, pos, vel, tr, exact=False, dt=p.dt)
 
 
 @pytest.mark.gpu
@@ -79,7 +79,7 @@ def test_fused_step_reproduces_reference(gpu, lib, path):
         else:
             tr["cell_start"] = s.fetch(pbfx.DBG_CELL_START)
             tr["cell_end"] = s.fetch(pbfx.DBG_CELL_END)
-    check_against(z, hashed, pos, vel, tr, exact=True)
+    check_against(z, hashed, pos, vel, tr, exact=True, dt=p.dt)
 
 
 @pytest.mark.gpu
