@@ -23,6 +23,8 @@ PBF_ERR_INVALID = 1
 PBF_ERR_CUDA = 2
 PBF_ERR_OOM = 3
 PBF_ERR_TIMEOUT = 4
+PBF_ERR_NONFINITE = 5
+PBF_ERR_UNSUPPORTED = 6
 PBF_GRID_DENSE = 0
 PBF_GRID_HASHED = 1
 
@@ -122,6 +124,7 @@ _SIGS = {
     "pbf_launch_cell_ranges": ([_VP, _VP, _VP, _U32, _U32, _VP], _I),
     "pbf_cell_compact_scratch_query": ([C.POINTER(_SZ), _U32], _I),
     "pbf_launch_cell_ranges_compact": ([_VP, _SZ, _VP, _VP, _VP, _VP, _U32, _VP], _I),
+    "pbf_launch_cell_ranges_compact_noalloc": ([_VP, _VP, _VP, _VP, _U32, _VP], _I),
     "pbf_launch_lambda": ([_VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
     "pbf_launch_lambda_compact": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),
     "pbf_launch_delta_apply": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(DeviceParams), _U32, _VP], _I),

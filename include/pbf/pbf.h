@@ -136,6 +136,22 @@ int pbf_launch_cell_ranges_compact(void* d_scratch, size_t scratchBytes,
                                    const uint32_t* keysSorted, uint32_t N,
                                    cudaStream_t s);
 
+/* No counterpart in the reference.  The same compaction as
+ * pbf_launch_cell_ranges_compact, for callers that cannot allocate device
+ * memory while they run (a frame loop where cudaMalloc/cudaFree would
+ * synchronize the device, a plugin host that hands out no GPU memory): its
+ * scratch is one fixed device array inside the library, so the caller passes
+ * only inputs and outputs.  At most 16,777,216 keys per call (larger N:
+ * PBF_ERR_UNSUPPORTED, nothing launched).  The first call on a device looks
+ * up the array's device address (once per device, with that device current);
+ * make that first call before any stream capture.  All calls share the array:
+ * each clears what must start at zero, but calls that overlap on the GPU
+ * race - serialize them. */
+int pbf_launch_cell_ranges_compact_noalloc(uint32_t* uniqueKeys, uint32_t* offsets,
+                                           uint32_t* compactCount,
+                                           const uint32_t* keysSorted, uint32_t N,
+                                           cudaStream_t s);
+
 /* sim/pbf_lambda.cu:246-258 LaunchLambda (dense table).  lambda[i] for every
  * particle i; the reference writes through device globals bound to the same
  * buffers, this entry point uses its arguments. */
