@@ -18,8 +18,9 @@ GPU vs the CPU oracle:
     1-2 ulps); velocities through the displacement they encode,
     |v_a - v_b| * dt <= STEP_POS * max|x| (v = (x - p) / dt turns one
     position ulp into 1/dt = 120 ulps of velocity); the last iteration's
-    lambda normwise (floor = max|lambda|) at STEP_LAMBDA, because those ulps
-    pass through the next solver iteration of the reference's ill-conditioned
+    lambda normwise (floor = max|lambda|) at STEP_LAMBDA per iteration after
+    the first (the ulps compound), because those ulps pass through the next
+    solver iteration of the reference's ill-conditioned
     displacement step (a sum of large cancelling terms that is then clamped
     to 0.05 h) and lambda = -C/denom with C = rho/rho0 - 1 near zero for many
     particles.
@@ -28,8 +29,12 @@ import numpy as np
 
 PHASE_DELTA = 1e-5  # normwise (floor = max|b|)
 STEP_POS = 1e-5
-STEP_LAMBDA = 1e-5  # normwise (floor = max|b|)
+STEP_LAMBDA = 1e-5  # normwise (floor = max|b|), per iteration after the first
 STEP_LAMBDA_FLOOR = 1.0
+
+
+def step_lambda_tol(iters):
+    return STEP_LAMBDA * max(1, iters - 1)
 
 
 def assert_velocities_close(v_a, v_b, pos_b, dt):

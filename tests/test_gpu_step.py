@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import pbfx
-from parity import STEP_LAMBDA, STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close
+from parity import STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close, step_lambda_tol
 
 pytestmark = pytest.mark.gpu
 
@@ -52,7 +52,7 @@ def compare_step(lib, orc, p, pos, vel, hashed, check_lambda=True):
         if iters == 1:
             np.testing.assert_array_equal(lam, tr["lambda"])  # from the prediction: exact
         else:
-            pbfx.assert_close(lam, tr["lambda"], STEP_LAMBDA, "lambda", floor_frac=STEP_LAMBDA_FLOOR)
+            pbfx.assert_close(lam, tr["lambda"], step_lambda_tol(iters), "lambda", floor_frac=STEP_LAMBDA_FLOOR)
     if iters == 0:
         np.testing.assert_array_equal(gpos, opos)
         np.testing.assert_array_equal(gvel, ovel)

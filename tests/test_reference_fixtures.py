@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 import pbfx
-from parity import STEP_LAMBDA, STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close
+from parity import STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close, step_lambda_tol
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
@@ -46,7 +46,7 @@ def check_against(z, hashed, out_pos, out_vel, tr, exact, dt):
         np.testing.assert_array_equal(out_vel, z["vel_out"])
     else:
         pbfx.assert_close(out_pos, z["pos_out"], STEP_POS, "positions")
-        pbfx.assert_close(tr["lambda"], z["lambda"], STEP_LAMBDA, "lambda", floor_frac=STEP_LAMBDA_FLOOR)
+        pbfx.assert_close(tr["lambda"], z["lambda"], step_lambda_tol(2), "lambda", floor_frac=STEP_LAMBDA_FLOOR)
         assert_velocities_close(out_vel, z["vel_out"], z["pos_out"], dt)
 
 
