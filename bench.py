@@ -88,6 +88,8 @@ def alg_bytes_per_particle(phase: str, n: int, num_cells: int, hashed: bool, ite
         return 16 + 4 + 4 + 16 + (32 if last else 0)  # R pred, lambda, key; W pred (+ R pos_s, W vel)
     if phase == "commit":
         return 16 + 16 + 4 + 4 + 16 + 16  # R pred, vel_s, key, perm; W pos, vel
+    if phase.startswith("lists"):
+        return 16 + 4  # R pred, key (the lists themselves are not algorithmic traffic)
     return 0.0
 
 
@@ -322,6 +324,7 @@ def run_ours(args, cfg, world, rank, local):
     e2e_s = time.perf_counter() - t0
     e2e_total, e2e_units = aggregate(e2e_s, float(n) * e2e_steps, world)
     launches = sim.launches_per_step() * args.steps
+    list_cap, list_longest, list_overflowed = sim.list_stats()
     sim.close()
 
     line = {
@@ -348,6 +351,7 @@ def run_ours(args, cfg, world, rank, local):
                     "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
         "gpu_launches": launches,
         "clocks": clk,
+        "neighbour_lists": {"capacity": list_cap, "longest": list_longest, "overflowed": list_overflowed},
     }
 
     # The reference's own CUDA kernels (compiled from its sources for sm_103a,

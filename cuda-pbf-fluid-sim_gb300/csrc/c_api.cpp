@@ -423,6 +423,23 @@ int pbf_profile_step(pbf_sim* h, const pbf_sim_params* p, float* ms, const char*
 
 int pbf_launches_per_step(pbf_sim* h) { return h ? h->sim.launchesPerStep() : 0; }
 
+int pbf_set_neighbour_list_capacity(pbf_sim* h, uint32_t entries) {
+    if (!h) return PBF_ERR_INVALID;
+    if (entries > (1u << 20)) return PBF_ERR_INVALID;
+    if (!h->sim.setNeighbourListCapacity(entries)) return PBF_ERR_OOM;
+    return PBF_OK;
+}
+
+int pbf_neighbour_list_stats(pbf_sim* h, uint32_t* capacity, uint32_t* longest, uint32_t* overflowed, int reset) {
+    if (!h) return PBF_ERR_INVALID;
+    uint32_t l = 0, o = 0;
+    if (!h->sim.neighbourListStats(l, o, reset != 0)) return PBF_ERR_CUDA;
+    if (capacity) *capacity = h->sim.neighbourListCapacity();
+    if (longest) *longest = l;
+    if (overflowed) *overflowed = o;
+    return PBF_OK;
+}
+
 int pbf_synchronize(pbf_sim* h) {
     if (!h) return PBF_ERR_INVALID;
     cudaError_t e = cudaStreamSynchronize(h->sim.cudaStream());

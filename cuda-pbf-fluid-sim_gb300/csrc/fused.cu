@@ -14,6 +14,10 @@
 //   k_commit         XSPH (Jacobi) + boundary(e) + scatter back to ids
 #include "fused.cuh"
 
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
 #include "grid.cuh"
 #include "pbf_common.cuh"
 #include "sort.cuh"
@@ -50,37 +54,346 @@ __global__ void __launch_bounds__(kBS) k_gather(const uint32_t* __restrict__ per
     pos_s[s] = p;
 }
 
-__global__ void __launch_bounds__(kNbrBS) k_lambda(const float4* __restrict__ pred, const uint32_t* __restrict__ key_s,
-                                                   const uint32_t* __restrict__ lb,
-                                                   const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                   float* __restrict__ lam) {
-    __shared__ uint32_t s_queue[kQueue * kNbrBS];
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+// Neighbour lists of one pass: the list built for the span this pass belongs
+// to (updates = position updates it covers; < 0: no list this pass).
+struct ListArgs {
+    const uint32_t* __restrict__ list;
+    const uint32_t* __restrict__ count;
+    uint32_t cap;
+    int updates;
+};
+
+// ------------------------------------------------------------- tiles
+// The list passes work on tiles of kTile consecutive sorted slots, one CTA
+// per tile.  When the tile's particles all lie in one (y, z) row of cells,
+// the union of their stencils is (2 reach + 1)^2 rows of cells, each one
+// contiguous slot range [start, start + len) covering the tile's x range
+// widened by reach.  If those ranges hold at most kStageMax slots, the
+// tile is "staged": every list pass copies the ranges into shared memory
+// (row r at base[r]) and the lists of its particles hold 16-bit indices
+// into that copy, so neighbour reads are shared-memory gathers.  Other tiles'
+// lists hold 32-bit sorted slots read from global memory.  The plan depends
+// only on the sorted keys, the lower-bound table and the grid, so the list
+// builder and every list pass derive the same one.
+constexpr int kTile = kNbrBS;
+constexpr int kStageMax = 1536;
+constexpr int kPlanRows = 32;
+static_assert(kStageMax <= 65536, "staged indices are 16-bit");
+
+struct TilePlan {
+    uint32_t start[kPlanRows];
+    uint32_t base[kPlanRows];
+    uint32_t len[kPlanRows];
+    uint32_t total;
+    int nrows;
+    int staged;
+};
+
+// A tile's plan as one warp holds it: lane r holds row r's range and stage
+// base.  Called by a whole warp.
+struct WarpPlan {
+    uint32_t start, base, len;  // this lane's row
+    uint32_t total;
+    int nrows;
+    bool staged;
+};
+
+__device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                   const sim::DeviceParams& dp, uint32_t t0, uint32_t N) {
+    const int lane = int(threadIdx.x & 31u);
+    const uint32_t tl = min(t0 + uint32_t(kTile), N) - 1u;
+    const int3 dim = dp.grid.dim;
+    int xf, yf, zf, xl, yl, zl;
+    decode_key(key_s[t0], dim, xf, yf, zf);
+    decode_key(key_s[tl], dim, xl, yl, zl);
+    const int reach = neighbour_reach(dp);
+    const int side = 2 * reach + 1;
+    WarpPlan w;
+    w.nrows = side * side;
+    // sorted keys: equal (y, z) at both ends means one row for the whole tile
+    const bool single = yf == yl && zf == zl && w.nrows <= kPlanRows;
+    w.start = 0;
+    w.len = 0;
+    if (single && lane < w.nrows) {
+        const int z = zf + lane / side - reach;
+        const int y = yf + lane % side - reach;
+        if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
+            const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
+            w.start = __ldg(lb + row + uint32_t(max(xf - reach, 0)));
+            w.len = __ldg(lb + row + uint32_t(min(xl + reach, dim.x - 1)) + 1u) - w.start;
+        }
+    }
+    uint32_t incl = w.len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    w.total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    w.base = incl - w.len;
+    w.staged = single && w.total <= uint32_t(kStageMax);
+    return w;
+}
+
+// The plan in shared memory for a CTA (written by warp 0).
+__device__ void plan_tile(TilePlan& P, const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                          const sim::DeviceParams& dp, uint32_t t0, uint32_t N) {
+    const WarpPlan w = plan_tile_warp(key_s, lb, dp, t0, N);
+    const int lane = int(threadIdx.x & 31u);
+    P.start[lane] = w.start;
+    P.base[lane] = w.base;
+    P.len[lane] = w.len;
+    if (lane == 0) {
+        P.total = w.total;
+        P.nrows = w.nrows;
+        P.staged = w.staged ? 1 : 0;
+    }
+}
+
+// Whether this pass may use lists (the builder decided the same from the same
+// parameters); CTA-uniform.
+__device__ __forceinline__ bool lists_usable(const ListArgs& la, const sim::DeviceParams& dp) {
+    float R2;
+    return la.updates >= 0 && la.cap > 0 && list_radius2(dp, la.updates, R2);
+}
+
+// Whether this warp walks its lists: no lane's list overflowed.  Every lane
+// must call it.
+__device__ __forceinline__ bool warp_lists_fit(const ListArgs& la, bool active, uint32_t sc, uint32_t& n) {
+    n = active ? la.count[sc] : 0u;
+    return !__any_sync(0xFFFFFFFFu, n > la.cap);
+}
+
+__device__ __forceinline__ RowSource row_source(const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                                const sim::DeviceParams& dp, uint32_t sc) {
+    RowSource r;
+    decode_key(key_s[sc], dp.grid.dim, r.cx, r.cy, r.cz);
+    r.reach = neighbour_reach(dp);
+    r.dim = dp.grid.dim;
+    r.lb = lb;
+    return r;
+}
+
+// Copies the tile's staged ranges into shared memory: sp[i] = (x, y, z, w)
+// with w = lam[k] when lam is given; with vel given, w = vel[k].x and
+// sv[i] = (vel[k].y, vel[k].z).  Every thread of the CTA calls it (between
+// barriers).
+__device__ __forceinline__ void stage_tile(const TilePlan& P, const float4* __restrict__ pos,
+                                           const float* __restrict__ lam, const float4* __restrict__ vel,
+                                           float4* sp, float2* sv) {
+    for (int r = 0; r < P.nrows; ++r) {
+        const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
+        for (uint32_t i = threadIdx.x; i < len; i += kTile) {
+            float4 x = __ldg(pos + st + i);
+            if (lam) x.w = __ldg(lam + st + i);
+            if (vel) {
+                const float4 v = __ldg(vel + st + i);
+                x.w = v.x;
+                sv[bs + i] = make_float2(v.y, v.z);
+            }
+            sp[bs + i] = x;
+        }
+    }
+}
+
+// Builds the neighbour lists: a warp takes its 32 particles one at a time,
+// 32 candidates per step, and a ballot compacts the candidates within the
+// list radius into the particle's list in walk order (coalesced stores).
+// Entries are 16-bit stage indices in staged tiles, 32-bit sorted slots
+// otherwise; each warp derives its tile's plan itself.
+constexpr int kBuildBS = 256;
+static_assert(kTile % 32 == 0, "tiles are whole warps");
+__global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restrict__ pred,
+                                                          const uint32_t* __restrict__ key_s,
+                                                          const uint32_t* __restrict__ lb,
+                                                          const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                          int updates, uint32_t cap, uint32_t* __restrict__ list,
+                                                          uint32_t* __restrict__ count, uint32_t* __restrict__ stats) {
+    const sim::DeviceParams& dp = *dpp;
+    float R2;
+    if (!list_radius2(dp, updates, R2)) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t s0 = (blockIdx.x * kBuildBS + threadIdx.x) & ~31u;
+    if (s0 >= N) return;  // warp-uniform
+    const WarpPlan plan = plan_tile_warp(key_s, lb, dp, s0 - s0 % uint32_t(kTile), N);
+    const bool staged = plan.staged;
+    const uint32_t planShift = plan.base - plan.start;  // lane r: stage index of slot k in row r is k + shift
+    const int reach = neighbour_reach(dp);
+    const int side = 2 * reach + 1;
+    const int nrows = side * side;
+    const int3 dim = dp.grid.dim;
+    const uint32_t lt = lanemask_lt();
+    uint32_t longest = 0, overflowed = 0;
+    const uint32_t pend = min(N - s0, 32u);
+    for (uint32_t p = 0; p < pend; ++p) {
+        const uint32_t s = s0 + p;
+        const float4 pi = pred[s];
+        int cx, cy, cz;
+        decode_key(key_s[s], dim, cx, cy, cz);
+        const int x0 = max(cx - reach, 0);
+        const int x1 = min(cx + reach, dim.x - 1);
+        uint32_t* out32 = list + size_t(s) * cap;
+        uint16_t* out16 = reinterpret_cast<uint16_t*>(out32);
+        uint32_t cnt = 0;
+        for (int r0 = 0; r0 < nrows; r0 += 32) {
+            // this batch's row ranges, one row per lane
+            const int r = r0 + int(lane);
+            uint32_t rb = 0, re = 0;
+            if (r < nrows) {
+                const int z = cz + r / side - reach;
+                const int y = cy + r % side - reach;
+                if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
+                    const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
+                    rb = __ldg(lb + row + uint32_t(x0));
+                    re = __ldg(lb + row + uint32_t(x1) + 1u);
+                }
+            }
+            const int nr = min(32, nrows - r0);
+            for (int rr = 0; rr < nr; ++rr) {
+                const uint32_t b = __shfl_sync(0xFFFFFFFFu, rb, rr);
+                const uint32_t e = __shfl_sync(0xFFFFFFFFu, re, rr);
+                // staged tiles have nrows <= 32, so r0 == 0 and the plan's lane rr is row rr
+                const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, rr);
+#pragma unroll 2
+                for (uint32_t c = b; c < e; c += 32u) {
+                    const uint32_t k = c + lane;
+                    bool in = false;
+                    if (k < e) {
+                        float rx, ry, rz;
+                        in = k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > R2);
+                    }
+                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+                    const uint32_t at = cnt + __popc(m & lt);
+                    if (in && at < cap) {
+                        if (staged)
+                            out16[at] = uint16_t(k + shift);
+                        else
+                            out32[at] = k;
+                    }
+                    cnt += __popc(m);
+                }
+            }
+        }
+        if (lane == 0) count[s] = cnt;
+        longest = max(longest, cnt);
+        overflowed += cnt > cap ? 1u : 0u;
+    }
+    if (lane == 0 && stats) {
+        atomicMax(stats, longest);
+        if (overflowed) atomicAdd(stats + 1, overflowed);
+    }
+}
+
+// Shared memory of the list passes.  lambda / delta: the stage (kStageMax
+// float4) then a queue of 16-bit stage indices (kQueue x kTile) for staged
+// tiles; tiles that are not staged keep 32-bit queues in the stage area.
+// XSPH: the stage as float4 (x, y, z, vx) plus float2 (vy, vz), its queue in
+// the stage area likewise.  In a staged tile a warp whose lists overflowed
+// walks the stencil in one pass, without a queue.
+constexpr size_t kStageBytes = size_t(kStageMax) * sizeof(float4);
+constexpr size_t kSolveSmem = kStageBytes + size_t(kQueue) * kTile * sizeof(uint16_t);
+constexpr size_t kCommitSmem = kStageBytes + size_t(kStageMax) * sizeof(float2);
+static_assert(size_t(kQueue) * kTile * sizeof(uint32_t) <= kStageBytes, "32-bit queues fit in the stage area");
+
+__global__ void __launch_bounds__(kTile) k_lambda(const float4* __restrict__ pred, const uint32_t* __restrict__ key_s,
+                                                  const uint32_t* __restrict__ lb,
+                                                  const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                  float* __restrict__ lam, ListArgs la) {
+    extern __shared__ float4 smem[];
+    __shared__ TilePlan P;
+    float4* sp = smem;
+    uint16_t* q16 = reinterpret_cast<uint16_t*>(smem + kStageMax) + threadIdx.x;
+    uint32_t* q32 = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
+    const uint32_t t0 = blockIdx.x * kTile;
+    const uint32_t s = t0 + threadIdx.x;
     const bool active = s < N;  // every lane takes part in the warp-wide rounds
     const uint32_t sc = active ? s : 0u;
     const sim::DeviceParams& dp = *dpp;
-    int cx, cy, cz;
-    decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
-    const float l = lambda_queued<kQueue, kNbrBS>(active, sc, pred[sc], cx, cy, cz, dp, lb, pred, s_queue + threadIdx.x);
+    const bool lists = lists_usable(la, dp);
+    if (lists) {
+        if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
+        __syncthreads();
+        if (P.staged) stage_tile(P, pred, nullptr, nullptr, sp, nullptr);
+        __syncthreads();
+    }
+    const bool staged = lists && P.staged;
+    const float4 pi = pred[sc];
+    const GlobalData g{pred, nullptr, nullptr};
+    uint32_t n;
+    float l = 0.f;
+    if (lists && warp_lists_fit(la, active, sc, n)) {
+        const uint32_t* base = la.list + size_t(sc) * la.cap;
+        if (staged)
+            l = lambda_queued<kQueue, kTile>(active, sc, pi,
+                                             ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                             StagedData{sp, nullptr}, q16);
+        else
+            l = lambda_queued<kQueue, kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
+    } else if (staged) {
+        int cx, cy, cz;
+        decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+        if (active)
+            l = lambda_of(sc, pi, cx, cy, cz, dp, LbRows{lb}, [&](uint32_t k, uint32_t& j) {
+                j = k;
+                return __ldg(pred + k);
+            });
+    } else {
+        l = lambda_queued<kQueue, kTile>(active, sc, pi, row_source(key_s, lb, dp, sc), dp, g, q32);
+    }
     if (active) lam[s] = l;
 }
 
 template <bool kLast>
-__global__ void __launch_bounds__(kNbrBS) k_delta(const float4* __restrict__ pred, const float* __restrict__ lam,
-                                                  const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                                  const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                  float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
-                                                  float4* __restrict__ vel_s) {
-    __shared__ uint32_t s_queue[kQueue * kNbrBS];
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kTile) k_delta(const float4* __restrict__ pred, const float* __restrict__ lam,
+                                                 const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                                 const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                 float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
+                                                 float4* __restrict__ vel_s, ListArgs la) {
+    extern __shared__ float4 smem[];
+    __shared__ TilePlan P;
+    float4* sp = smem;
+    uint16_t* q16 = reinterpret_cast<uint16_t*>(smem + kStageMax) + threadIdx.x;
+    uint32_t* q32 = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
+    const uint32_t t0 = blockIdx.x * kTile;
+    const uint32_t s = t0 + threadIdx.x;
     const bool active = s < N;  // every lane takes part in the warp-wide rounds
     const uint32_t sc = active ? s : 0u;
     const sim::DeviceParams& dp = *dpp;
-    int cx, cy, cz;
-    decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+    const bool lists = lists_usable(la, dp);
+    if (lists) {
+        if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
+        __syncthreads();
+        if (P.staged) stage_tile(P, pred, lam, nullptr, sp, nullptr);
+        __syncthreads();
+    }
+    const bool staged = lists && P.staged;
     const float4 pi = pred[sc];
-    const float3 d = delta_queued<kQueue, kNbrBS>(active, sc, pi, lam[sc], cx, cy, cz, dp, scorr_wq(dp), lb, pred,
-                                                   lam, s_queue + threadIdx.x);
+    const float lam_i = lam[sc];
+    const float w_q = scorr_wq(dp);
+    const GlobalData g{pred, lam, nullptr};
+    uint32_t n;
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    if (lists && warp_lists_fit(la, active, sc, n)) {
+        const uint32_t* base = la.list + size_t(sc) * la.cap;
+        if (staged)
+            d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i,
+                                            ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                            w_q, StagedData{sp, nullptr}, q16);
+        else
+            d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
+                                            q32);
+    } else if (staged) {
+        int cx, cy, cz;
+        decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+        if (active)
+            d = delta_of(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb}, [&](uint32_t k, uint32_t& j, float& lj) {
+                j = k;
+                lj = __ldg(lam + k);
+                return __ldg(pred + k);
+            });
+    } else {
+        d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i, row_source(key_s, lb, dp, sc), dp, w_q, g, q32);
+    }
     if (!active) return;
     float4 x = make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w);
     if (kLast) {
@@ -114,22 +427,57 @@ __global__ void __launch_bounds__(kBS) k_finalize_no_iters(float4* __restrict__ 
 }
 
 template <bool kXsph>
-__global__ void __launch_bounds__(kNbrBS) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
-                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                                   const uint32_t* __restrict__ perm,
-                                                   const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                   float4* __restrict__ pos, float4* __restrict__ vel) {
-    __shared__ uint32_t s_queue[kXsph ? kQueue * kNbrBS : 1];
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
+                                                  const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                                  const uint32_t* __restrict__ perm,
+                                                  const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                  float4* __restrict__ pos, float4* __restrict__ vel, ListArgs la) {
+    extern __shared__ float4 smem[];
+    __shared__ TilePlan P;
+    const uint32_t t0 = blockIdx.x * kTile;
+    const uint32_t s = t0 + threadIdx.x;
     const bool active = s < N;  // every lane takes part in the warp-wide rounds
     const uint32_t sc = active ? s : 0u;
     const sim::DeviceParams& dp = *dpp;
     float4 x = pred[sc];
     float4 v = vel_s[sc];
     if (kXsph && dp.xsph_c > 0.f) {
-        int cx, cy, cz;
-        decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
-        v = xsph_queued<kQueue, kNbrBS>(active, sc, x, v, cx, cy, cz, dp, lb, pred, vel_s, s_queue + threadIdx.x);
+        float4* sp = smem;
+        float2* sv = reinterpret_cast<float2*>(smem + kStageMax);
+        const bool lists = lists_usable(la, dp);
+        if (lists) {
+            if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
+            __syncthreads();
+            if (P.staged) stage_tile(P, pred, nullptr, vel_s, sp, sv);
+            __syncthreads();
+        }
+        const bool staged = lists && P.staged;
+        // Queue of the queued walks: the stage area, free in tiles that are
+        // not staged.  In a staged tile a warp whose lists overflowed walks
+        // the stencil without a queue.
+        uint32_t* q = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
+        const GlobalData g{pred, nullptr, vel_s};
+        uint32_t n;
+        if (lists && warp_lists_fit(la, active, sc, n)) {
+            const uint32_t* base = la.list + size_t(sc) * la.cap;
+            if (staged)
+                v = xsph_list_inline(active, x, v,
+                                     ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                     StagedData{sp, sv});
+            else
+                v = xsph_queued<kQueue, kTile>(active, sc, x, v, ListSource<uint32_t>{base, n, sc}, dp, g, q);
+        } else if (staged) {
+            int cx, cy, cz;
+            decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+            if (active)
+                v = xsph_of(sc, x, v, cx, cy, cz, dp, LbRows{lb}, [&](uint32_t k, uint32_t& j, float4& vj) {
+                    j = k;
+                    vj = __ldg(vel_s + k);
+                    return __ldg(pred + k);
+                });
+        } else {
+            v = xsph_queued<kQueue, kTile>(active, sc, x, v, row_source(key_s, lb, dp, sc), dp, g, q);
+        }
     }
     if (!active) return;
     boundary_apply(x, v, dp.grid, dp.boundaryRestitution);
@@ -260,18 +608,108 @@ cudaError_t fused_gather_and_tables(const FusedBufs& b, const FusedShape& sh, cu
     return cudaGetLastError();
 }
 
+int list_span_for(const sim::SimParams& p) {
+    if (!p.pbf.enable_disp_clamp || p.solverIters <= 0) return 0;
+    const float md = std::fabs(p.pbf.disp_clamp_max_h);
+    if (!(md < 1.0f)) return 0;  // NaN, or updates move particles by h or more
+    const int iters = p.solverIters;
+    // One list for the whole step while its radius h + 2 * iters * md stays
+    // within 1.5 h.
+    if (2.0f * float(iters) * md <= 0.5f) return iters;
+    // Otherwise a list per span of iterations whose lambda / delta passes read
+    // at most span - 1 updates after the build (radius <= 1.25 h); the commit
+    // then walks the stencil.
+    const int span = int(0.125f / md) + 1;
+    return span >= 2 ? std::min(span, iters - 1) : 0;
+}
+
+namespace {
+
+bool lists_on(const FusedBufs& b, const FusedShape& sh) {
+    return sh.list_span > 0 && b.nbr_cap > 0 && b.nbr_list && b.nbr_count && sh.iters > 0;
+}
+
+// Position updates the list serving iteration `it` (it == iters: the commit)
+// must cover, or -1 when that pass walks the stencil.
+//   * One list (span >= iters): built from the prediction p0, which lies in
+//     the box; the passes read p0 .. p_{iters-1} and the commit reads
+//     p_iters = P(p0 + D), P the projection onto the box, and since
+//     |P(p0 + D) - p0| = |P(p0 + D) - P(p0)| <= |D|, every pass is within
+//     iters clamped updates of p0.
+//   * A list per span: a span's lambda / delta passes read the predictions
+//     p_start .. p_{start+span-1}, no boundary in between, so span - 1
+//     updates.  The commit is not covered: p_start may lie outside the box
+//     and the final projection may move it further than the remaining
+//     updates.
+int list_updates(const FusedShape& sh, int it) {
+    if (sh.list_span >= sh.iters) return sh.iters;
+    return it >= sh.iters ? -1 : sh.list_span - 1;
+}
+
+ListArgs list_args(const FusedBufs& b, const FusedShape& sh, int it) {
+    ListArgs la{b.nbr_list, b.nbr_count, b.nbr_cap, -1};
+    if (lists_on(b, sh)) la.updates = list_updates(sh, it);
+    return la;
+}
+
+}  // namespace
+
+int fused_list_builds(const FusedShape& sh) {
+    if (sh.list_span <= 0 || sh.iters <= 0) return 0;
+    return (sh.iters + sh.list_span - 1) / sh.list_span;
+}
+
+// Opts the list passes into their dynamic shared memory (above the 48 KB
+// default); once per process and device, before the first launch or capture.
+cudaError_t fused_prepare_kernels() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return cudaSuccess;
+    const int solve = int(kSolveSmem), commit = int(kCommitSmem);
+    if ((e = cudaFuncSetAttribute(k_lambda, cudaFuncAttributeMaxDynamicSharedMemorySize, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, commit)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, commit)) !=
+            cudaSuccess)
+        return e;
+    done[dev] = true;
+    return cudaSuccess;
+}
+
+cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, cudaStream_t s) {
+    if (sh.N == 0 || !lists_on(b, sh) || it < 0 || it >= sh.iters || it % sh.list_span != 0) return cudaErrorNotReady;
+    const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
+    k_build_lists<<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(cur, b.key_s, b.lb, b.dp, sh.N,
+                                                                 list_updates(sh, it), b.nbr_cap, b.nbr_list,
+                                                                 b.nbr_count, b.nbr_stats);
+    return cudaGetLastError();
+}
+
 cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, int which, cudaStream_t s) {
     if (sh.N == 0 || it < 0 || it >= sh.iters) return cudaSuccess;
-    const unsigned g = blocks_for(sh.N, kNbrBS);
+    cudaError_t e = fused_prepare_kernels();
+    if (e != cudaSuccess) return e;
+    const unsigned g = blocks_for(sh.N, kTile);
     // iteration it reads buffer (it even ? a : b) and writes the other one
     float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
     float4* nxt = (it % 2 == 0) ? b.pred_b : b.pred_a;
+    const ListArgs la = list_args(b, sh, it);
     if (which == 0) {
-        k_lambda<<<g, kNbrBS, 0, s>>>(cur, b.key_s, b.lb, b.dp, sh.N, b.lam_s);
+        k_lambda<<<g, kTile, kSolveSmem, s>>>(cur, b.key_s, b.lb, b.dp, sh.N, b.lam_s, la);
     } else if (it == sh.iters - 1) {
-        k_delta<true><<<g, kNbrBS, 0, s>>>(cur, b.lam_s, b.key_s, b.lb, b.dp, sh.N, nxt, b.pos_s, b.vel_s);
+        k_delta<true><<<g, kTile, kSolveSmem, s>>>(cur, b.lam_s, b.key_s, b.lb, b.dp, sh.N, nxt, b.pos_s, b.vel_s,
+                                                   la);
     } else {
-        k_delta<false><<<g, kNbrBS, 0, s>>>(cur, b.lam_s, b.key_s, b.lb, b.dp, sh.N, nxt, b.pos_s, b.vel_s);
+        k_delta<false><<<g, kTile, kSolveSmem, s>>>(cur, b.lam_s, b.key_s, b.lb, b.dp, sh.N, nxt, b.pos_s, b.vel_s,
+                                                    la);
     }
     return cudaGetLastError();
 }
@@ -279,6 +717,8 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
 cudaError_t fused_solve(const FusedBufs& b, const FusedShape& sh, cudaStream_t s) {
     if (sh.N == 0) return cudaSuccess;
     for (int it = 0; it < sh.iters; ++it) {
+        const cudaError_t e = fused_build_lists(b, sh, it, s);
+        if (e != cudaSuccess && e != cudaErrorNotReady) return e;
         fused_solve_phase(b, sh, it, 0, s);
         fused_solve_phase(b, sh, it, 1, s);
     }
@@ -289,12 +729,16 @@ cudaError_t fused_solve(const FusedBufs& b, const FusedShape& sh, cudaStream_t s
 
 cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t s) {
     if (sh.N == 0) return cudaSuccess;
+    cudaError_t e = fused_prepare_kernels();
+    if (e != cudaSuccess) return e;
     const float4* x = fused_final_pred(b, sh);
-    const unsigned g = blocks_for(sh.N, kNbrBS);
+    const unsigned g = blocks_for(sh.N, kTile);
+    const ListArgs la = list_args(b, sh, sh.iters);
     if (sh.xsph)
-        k_commit<true><<<g, kNbrBS, 0, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, b.dp, sh.N, b.pos, b.vel);
+        k_commit<true><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, b.dp, sh.N, b.pos, b.vel, la);
     else
-        k_commit<false><<<g, kNbrBS, 0, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, b.dp, sh.N, b.pos, b.vel);
+        k_commit<false><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, b.dp, sh.N, b.pos, b.vel,
+                                                      la);
     return cudaGetLastError();
 }
 

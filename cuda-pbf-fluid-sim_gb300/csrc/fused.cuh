@@ -44,6 +44,15 @@ struct FusedBufs {
     uint32_t* err;                // device error word
     double* stats_partials;       // device, >= kStatsMaxBlocks * 4 doubles
     double* stats_out;            // device, 4 doubles
+    // Neighbour lists (cell order): particle s owns entries
+    // nbr_list[s * nbr_cap, (s + 1) * nbr_cap); nbr_count[s] is its length
+    // (> nbr_cap: overflowed, the particle's warp walks the stencil instead).
+    // nbr_stats[0] = longest list built, nbr_stats[1] = overflowed lists
+    // (both accumulate until the host clears them).
+    uint32_t* nbr_list;
+    uint32_t* nbr_count;
+    uint32_t* nbr_stats;
+    uint32_t nbr_cap;  // entries per particle, a multiple of 8; 0 = no lists
 };
 
 struct FusedShape {
@@ -53,9 +62,23 @@ struct FusedShape {
     int iters;
     bool hashed;
     bool xsph;
+    // Solver iterations one neighbour list covers (lists are built before
+    // lambda of iterations 0, span, 2*span, ...); 0 = every pass walks the
+    // stencil.
+    int list_span;
 };
 
+// Iterations a list may cover for these parameters: the list radius grows by
+// 2 * disp_clamp_max_h * h per covered position update; lists are rebuilt
+// once it would pass 1.25 h.  0 when the displacement clamp is off (no bound
+// on how far particles move, so no list is valid).
+int list_span_for(const sim::SimParams& p);
+
 constexpr unsigned kStatsMaxBlocks = 1024;
+
+// One-time per-device kernel setup (shared-memory opt-in of the list passes);
+// the launchers call it too, but it must first run outside stream capture.
+cudaError_t fused_prepare_kernels();
 
 // Phase launchers of the fused step (each one graph-capturable).
 cudaError_t fused_predict_keys(const FusedBufs& b, const FusedShape& sh, cudaStream_t s);
@@ -64,8 +87,14 @@ cudaError_t fused_gather_and_tables(const FusedBufs& b, const FusedShape& sh, cu
 cudaError_t fused_solve(const FusedBufs& b, const FusedShape& sh, cudaStream_t s);
 cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t s);
 // One kernel of the solve loop: iteration `it`, which = 0 (lambda) or 1
-// (delta).  fused_solve == all of them in order.
+// (delta).  fused_solve == all of them in order, each iteration's lambda
+// preceded by fused_build_lists.
 cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, int which, cudaStream_t s);
+// Builds the neighbour lists if iteration `it` starts a list span; returns
+// cudaErrorNotReady (and launches nothing) when it does not.
+cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, cudaStream_t s);
+// Number of list builds per step.
+int fused_list_builds(const FusedShape& sh);
 // Sorted buffer holding the solved prediction after fused_solve.
 inline float4* fused_final_pred(const FusedBufs& b, const FusedShape& sh) {
     return (sh.iters % 2 == 0) ? b.pred_a : b.pred_b;

@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "../../include/pbf/parameters.h"
@@ -237,15 +238,6 @@ __device__ __forceinline__ void walk_queued(bool active, int cx, int cy, int cz,
     }
 }
 
-// r^2 of a candidate as the reference's neighbour loops compute it
-// (sim/pbf_lambda.cu:67-68).
-__device__ __forceinline__ float dist2(float4 pi, float4 pj, float& rx, float& ry, float& rz) {
-    rx = sub_(pi.x, pj.x);
-    ry = sub_(pi.y, pj.y);
-    rz = sub_(pi.z, pj.z);
-    return sumsq_(rx, ry, rz);
-}
-
 // Row ranges from a dense lower-bound table lb[c] = first sorted slot whose
 // key >= c (numCells+1 entries).
 struct LbRows {
@@ -254,6 +246,151 @@ struct LbRows {
         return make_uint2(__ldg(lb + c0), __ldg(lb + c1 + 1u));
     }
 };
+
+// ------------------------------------------------------ neighbour lists
+// The walk cell of a particle is its start-of-step cell for the whole step,
+// so its candidates (the stencil's slot ranges) are fixed; only positions
+// move, and with the displacement clamp on each solver update moves a
+// particle by at most maxDisp = disp_clamp_max_h * h.  A list of the
+// candidates within R = h + 2 * updates * maxDisp (plus rounding margins) of
+// the particle, in walk order, therefore holds every candidate that a pass
+// whose positions are within `updates` clamped moves of the list's accepts
+// (r^2 <= h^2), and filtering it with the reference's test yields exactly the
+// full walk's neighbours in the full walk's order.  (Which passes a list may
+// serve, given the box projection after the last update, is decided by the
+// host schedule.)  Returns false (lists unusable) when the clamp is off or the
+// radius is not finite; builders and users of a list call this with the same
+// arguments and so agree.
+__device__ __forceinline__ bool list_radius2(const sim::DeviceParams& dp, int updates, float& R2) {
+    if (!dp.pbf.enable_disp_clamp || updates < 0) return false;
+    const float h = dp.kernel.h;
+    const float md = fabsf(dp.pbf.disp_clamp_max_h * h);
+    const sim::GridBounds& g = dp.grid;
+    // Rounding of x + d: half an ulp of |x| per component; |x| <= box + h +
+    // iters * md, and the 0.1% slack on md absorbs the iters * md part for
+    // any iteration count below 2000.
+    const float box = fmaxf(fmaxf(fmaxf(fabsf(g.mins.x), fabsf(g.maxs.x)), fmaxf(fabsf(g.mins.y), fabsf(g.maxs.y))),
+                            fmaxf(fabsf(g.mins.z), fabsf(g.maxs.z)));
+    const float perUpdate = md * 1.001f + (box + h) * 4.8e-7f;
+    const float R = h * 1.001f + 2.0f * float(updates) * perUpdate;
+    R2 = R * R * 1.001f;
+    return h > 0.f && isfinite(R2) && R2 >= dp.kernel.h2;
+}
+
+// Eight consecutive list entries (32-bit sorted slots or 16-bit indices into
+// a staged tile) from a 16-byte aligned address.
+__device__ __forceinline__ void load8(const uint32_t* __restrict__ p, uint32_t (&k)[8]) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+    const uint4 b = __ldg(reinterpret_cast<const uint4*>(p) + 1);
+    k[0] = a.x; k[1] = a.y; k[2] = a.z; k[3] = a.w;
+    k[4] = b.x; k[5] = b.y; k[6] = b.z; k[7] = b.w;
+}
+__device__ __forceinline__ void load8(const uint16_t* __restrict__ p, uint32_t (&k)[8]) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+    k[0] = a.x & 0xFFFFu; k[1] = a.x >> 16; k[2] = a.y & 0xFFFFu; k[3] = a.y >> 16;
+    k[4] = a.z & 0xFFFFu; k[5] = a.z >> 16; k[6] = a.w & 0xFFFFu; k[7] = a.w >> 16;
+}
+
+// A particle's neighbour list: n entries in walk order (E = uint32_t: sorted
+// slots; E = uint16_t: indices into the tile staged in shared memory).  The
+// list is 16-byte aligned with at least round_up(n, 8) readable entries.
+// `fill` is an index that is safe to read and is used by lanes past their
+// list's end (their results are discarded).
+template <class E>
+struct ListSource {
+    const E* __restrict__ lst;
+    uint32_t n;
+    uint32_t fill;
+};
+
+// Lockstep walk over a neighbour list with the same queueing and draining as
+// walk_queued, over a flat candidate sequence.
+template <int Q, int kStride, class E, class QT, class Hit, class Body>
+__device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E>& src, QT* q, int maxHits,
+                                                 Hit&& hit, Body&& body) {
+    constexpr int kChunk = 8;
+    static_assert(Q > kChunk, "queue must hold more than one chunk");
+    int cnt = 0, total = 0;
+    uint32_t e = 0;
+    const uint32_t n = src.n;
+    bool done = !active || n == 0;
+    for (;;) {
+        const bool any = __any_sync(0xFFFFFFFFu, !done);
+        if (!done) {
+            uint32_t ks[kChunk];
+            load8(src.lst + e, ks);
+#pragma unroll
+            for (int u = 0; u < kChunk; ++u) {
+                const bool v = !done && e + uint32_t(u) < n;
+                const uint32_t k = v ? ks[u] : src.fill;
+                const bool h = v && hit(k);
+                q[cnt * kStride] = QT(k);  // cnt <= Q - 1 here: the queue holds <= Q - kChunk at a chunk's start
+                cnt += h ? 1 : 0;
+                total += h ? 1 : 0;
+                done = done || total >= maxHits;
+            }
+            e += kChunk;
+            done = done || e >= n;
+        }
+        if (!any || __any_sync(0xFFFFFFFFu, cnt > Q - kChunk)) {
+            for (int j = 0; j < cnt; ++j) body(q[j * kStride]);
+            cnt = 0;
+            if (!any) break;
+        }
+    }
+}
+
+// Candidate sources of the queued passes: the stencil's rows, or a list.
+struct RowSource {
+    int cx, cy, cz, reach;
+    int3 dim;
+    const uint32_t* __restrict__ lb;
+};
+
+template <int Q, int kStride, class QT, class Hit, class Body>
+__device__ __forceinline__ void walk_source(bool active, const RowSource& r, QT* q, int maxHits, Hit&& hit,
+                                            Body&& body) {
+    static_assert(std::is_same<QT, uint32_t>::value, "stencil walks queue 32-bit slots");
+    walk_queued<Q, kStride>(active, r.cx, r.cy, r.cz, r.reach, r.dim, LbRows{r.lb}, q, maxHits, hit, body);
+}
+template <int Q, int kStride, class E, class QT, class Hit, class Body>
+__device__ __forceinline__ void walk_source(bool active, const ListSource<E>& l, QT* q, int maxHits, Hit&& hit,
+                                            Body&& body) {
+    walk_list_queued<Q, kStride>(active, l, q, maxHits, hit, body);
+}
+
+// Where the queued passes read a candidate's data: the cell-ordered arrays in
+// global memory, or a tile staged in shared memory (x, y, z, lambda) plus
+// velocities.
+struct GlobalData {
+    const float4* __restrict__ pos;
+    const float* __restrict__ lam;
+    const float4* __restrict__ vel;
+    __device__ __forceinline__ float4 p(uint32_t k) const { return __ldg(pos + k); }
+    __device__ __forceinline__ float l(uint32_t k, const float4&) const { return __ldg(lam + k); }
+    __device__ __forceinline__ float4 v(uint32_t k) const { return __ldg(vel + k); }
+};
+// Staged tile in shared memory: p_[k] = (x, y, z, w) with w = lambda (delta
+// passes) or the x velocity (XSPH, whose y and z velocities are in v_[k]).
+struct StagedData {
+    const float4* p_;
+    const float2* v_;
+    __device__ __forceinline__ float4 p(uint32_t k) const { return p_[k]; }
+    __device__ __forceinline__ float l(uint32_t, const float4& pj) const { return pj.w; }
+    __device__ __forceinline__ float4 v(uint32_t k) const {
+        const float2 yz = v_[k];
+        return make_float4(p_[k].w, yz.x, yz.y, 0.f);
+    }
+};
+
+// r^2 of a candidate as the reference's neighbour loops compute it
+// (sim/pbf_lambda.cu:67-68).
+__device__ __forceinline__ float dist2(float4 pi, float4 pj, float& rx, float& ry, float& rz) {
+    rx = sub_(pi.x, pj.x);
+    ry = sub_(pi.y, pj.y);
+    rz = sub_(pi.z, pj.z);
+    return sumsq_(rx, ry, rz);
+}
 
 // Row ranges from the reference's dense table (start = 0xFFFFFFFF and
 // end = 0 for empty cells): min of starts, max of ends.
@@ -361,23 +498,26 @@ __device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int
     return lambda_finalize(a, dp);
 }
 
-// Two-phase walk over cell-ordered positions (slot k is particle k).
-template <int Q, int kStride>
-__device__ __forceinline__ float lambda_queued(bool active, uint32_t s, float4 pi, int cx, int cy, int cz,
-                                               const sim::DeviceParams& dp, const uint32_t* __restrict__ lb,
-                                               const float4* __restrict__ pred, uint32_t* q) {
+// Two-phase walk over cell-ordered positions (slot k is particle k); Src is
+// RowSource (the stencil) or a ListSource, Data GlobalData or StagedData.
+// Stencil candidates include the particle itself (rejected by slot); lists
+// never do.
+template <int Q, int kStride, class Src, class Data, class QT>
+__device__ __forceinline__ float lambda_queued(bool active, uint32_t s, float4 pi, const Src& src,
+                                               const sim::DeviceParams& dp, const Data& data, QT* q) {
     LambdaAcc a;
     const int cap = dp.maxNeighbors;
     const float h2 = dp.kernel.h2;
-    walk_queued<Q, kStride>(
-        active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, q, cap > 0 ? cap : 0x7FFFFFFF,
+    constexpr bool kSelf = std::is_same<Src, RowSource>::value;
+    walk_source<Q, kStride>(
+        active, src, q, cap > 0 ? cap : 0x7FFFFFFF,
         [&](uint32_t k) -> bool {
             float rx, ry, rz;
-            return k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > h2);
+            return (!kSelf || k != s) && !(dist2(pi, data.p(k), rx, ry, rz) > h2);
         },
         [&](uint32_t k) {
             float rx, ry, rz;
-            const float r2 = dist2(pi, __ldg(pred + k), rx, ry, rz);
+            const float r2 = dist2(pi, data.p(k), rx, ry, rz);
             lambda_accumulate(a, rx, ry, rz, r2, dp);
         });
     return lambda_finalize(a, dp);
@@ -462,23 +602,23 @@ __device__ __forceinline__ float3 delta_of(uint32_t self, float4 pi, float lam_i
     return delta_finalize(dsum, dp);
 }
 
-template <int Q, int kStride>
-__device__ __forceinline__ float3 delta_queued(bool active, uint32_t s, float4 pi, float lam_i, int cx, int cy, int cz,
-                                               const sim::DeviceParams& dp, float w_q,
-                                               const uint32_t* __restrict__ lb, const float4* __restrict__ pred,
-                                               const float* __restrict__ lam, uint32_t* q) {
+template <int Q, int kStride, class Src, class Data, class QT>
+__device__ __forceinline__ float3 delta_queued(bool active, uint32_t s, float4 pi, float lam_i, const Src& src,
+                                               const sim::DeviceParams& dp, float w_q, const Data& data, QT* q) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
     const float h2 = dp.kernel.h2;
-    walk_queued<Q, kStride>(
-        active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, q, 0x7FFFFFFF,
+    constexpr bool kSelf = std::is_same<Src, RowSource>::value;
+    walk_source<Q, kStride>(
+        active, src, q, 0x7FFFFFFF,
         [&](uint32_t k) -> bool {
             float rx, ry, rz;
-            return k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > h2);
+            return (!kSelf || k != s) && !(dist2(pi, data.p(k), rx, ry, rz) > h2);
         },
         [&](uint32_t k) {
             float rx, ry, rz;
-            const float r2 = dist2(pi, __ldg(pred + k), rx, ry, rz);
-            delta_accumulate(dsum, rx, ry, rz, r2, lam_i, __ldg(lam + k), w_q, dp);
+            const float4 pj = data.p(k);
+            const float r2 = dist2(pi, pj, rx, ry, rz);
+            delta_accumulate(dsum, rx, ry, rz, r2, lam_i, data.l(k, pj), w_q, dp);
         });
     return delta_finalize(dsum, dp);
 }
@@ -529,25 +669,50 @@ __device__ __forceinline__ float4 xsph_of(uint32_t self, float4 pi, float4 vi, i
     return xsph_finalize(sum, count, vi, dp);
 }
 
-template <int Q, int kStride>
-__device__ __forceinline__ float4 xsph_queued(bool active, uint32_t s, float4 pi, float4 vi, int cx, int cy, int cz,
-                                              const sim::DeviceParams& dp, const uint32_t* __restrict__ lb,
-                                              const float4* __restrict__ pred, const float4* __restrict__ vel,
-                                              uint32_t* q) {
+template <int Q, int kStride, class Src, class Data, class QT>
+__device__ __forceinline__ float4 xsph_queued(bool active, uint32_t s, float4 pi, float4 vi, const Src& src,
+                                              const sim::DeviceParams& dp, const Data& data, QT* q) {
     float3 sum = make_float3(0.f, 0.f, 0.f);
     int count = 0;
     const float h2 = dp.kernel.h2;
-    walk_queued<Q, kStride>(
-        active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, q, 0x7FFFFFFF,
+    constexpr bool kSelf = std::is_same<Src, RowSource>::value;
+    walk_source<Q, kStride>(
+        active, src, q, 0x7FFFFFFF,
         [&](uint32_t k) -> bool {
             float rx, ry, rz;
-            return k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > h2);
+            return (!kSelf || k != s) && !(dist2(pi, data.p(k), rx, ry, rz) > h2);
         },
         [&](uint32_t k) {
             float rx, ry, rz;
-            const float r2 = dist2(pi, __ldg(pred + k), rx, ry, rz);
-            xsph_accumulate(sum, count, r2, vi, __ldg(vel + k), dp);
+            const float r2 = dist2(pi, data.p(k), rx, ry, rz);
+            xsph_accumulate(sum, count, r2, vi, data.v(k), dp);
         });
+    return xsph_finalize(sum, count, vi, dp);
+}
+
+// XSPH over a list with the body inline (no queue): for light bodies over
+// data staged in shared memory, where re-reading candidates is not worth a
+// queue.
+template <class E, class Data>
+__device__ __forceinline__ float4 xsph_list_inline(bool active, float4 pi, float4 vi, const ListSource<E>& src,
+                                                   const sim::DeviceParams& dp, const Data& data) {
+    float3 sum = make_float3(0.f, 0.f, 0.f);
+    int count = 0;
+    const float h2 = dp.kernel.h2;
+    const uint32_t n = active ? src.n : 0u;
+    for (uint32_t e = 0; e < n; e += 8) {
+        uint32_t ks[8];
+        load8(src.lst + e, ks);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (e + uint32_t(u) < n) {
+                float rx, ry, rz;
+                const uint32_t k = ks[u];
+                const float r2 = dist2(pi, data.p(k), rx, ry, rz);
+                if (!(r2 > h2)) xsph_accumulate(sum, count, r2, vi, data.v(k), dp);
+            }
+        }
+    }
     return xsph_finalize(sum, count, vi, dp);
 }
 

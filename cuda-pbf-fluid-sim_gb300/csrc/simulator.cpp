@@ -64,6 +64,10 @@ pbf::FusedBufs fused_bufs(DeviceBuffers& b, GridBuffers& g) {
     f.err = b.d_err;
     f.stats_out = b.d_stats;
     f.stats_partials = b.d_stats + 4;
+    f.nbr_list = b.d_nbrList;
+    f.nbr_count = b.d_nbrCount;
+    f.nbr_stats = b.d_nbrStats;
+    f.nbr_cap = b.nbrListCap;
     return f;
 }
 
@@ -75,6 +79,7 @@ pbf::FusedShape fused_shape(const DeviceBuffers& b, const GridBuffers& g, const 
     s.iters = p.solverIters;
     s.hashed = g.hashed;
     s.xsph = b.xsphEnabled;
+    s.list_span = pbf::list_span_for(p);
     return s;
 }
 
@@ -140,7 +145,30 @@ bool DeviceBuffers::allocate(uint32_t cap) {
     return true;
 }
 
+bool DeviceBuffers::allocateLists(uint32_t entries) {
+    releaseLists();
+    entries = (entries + 7u) & ~7u;
+    if (entries == 0 || capacity == 0) return true;
+    const size_t n = size_t(capacity) * entries;
+    if (!dalloc(&d_nbrList, n) || !dalloc(&d_nbrCount, capacity) || !dalloc(&d_nbrStats, 2)) {
+        releaseLists();
+        cudaGetLastError();
+        return false;
+    }
+    cudaMemset(d_nbrStats, 0, 2 * sizeof(uint32_t));
+    nbrListCap = entries;
+    return true;
+}
+
+void DeviceBuffers::releaseLists() {
+    dfree(d_nbrList);
+    dfree(d_nbrCount);
+    dfree(d_nbrStats);
+    nbrListCap = 0;
+}
+
 void DeviceBuffers::release() {
+    releaseLists();
     dfree(d_pos);
     dfree(d_vel);
     dfree(d_pos_pred);
@@ -228,6 +256,7 @@ void ParamChangeTracker::capture(const SimParams& p, uint32_t numCells) {
     m_numCells = numCells;
     m_grid = p.grid;
     m_xsph = p.xsph_c > 0.f;
+    m_listSpan = pbf::list_span_for(p);
 }
 
 bool ParamChangeTracker::structuralChanged(const SimParams& p, uint32_t numCells) const {
@@ -236,6 +265,7 @@ bool ParamChangeTracker::structuralChanged(const SimParams& p, uint32_t numCells
     if (p.numParticles != m_numParticles) return true;
     if (numCells != m_numCells) return true;
     if (p.grid.dim.x != m_grid.dim.x || p.grid.dim.y != m_grid.dim.y || p.grid.dim.z != m_grid.dim.z) return true;
+    if (pbf::list_span_for(p) != m_listSpan) return true;  // list builds are part of the graph
     return false;
 }
 
@@ -255,6 +285,8 @@ bool Simulator::initialize(const SimParams& p, bool useHashedGrid) {
     if (cap == 0) cap = 1;
     if (!m_bufs.allocate(cap)) return false;
     if (!m_grid.allocate(cap, nc)) return false;
+    m_bufs.allocateLists(m_listCapacity);  // lists stay off if this fails
+    if (pbf::fused_prepare_kernels() != cudaSuccess) return false;
     m_grid.hashed = useHashedGrid;
     m_bufs.xsphEnabled = (p.xsph_c > 0.f);
     m_kernelDispatcher = KernelDispatcher{};
@@ -311,6 +343,7 @@ bool Simulator::ensureCapacity(uint32_t n) {
     cudaMemcpy(vel.data(), m_bufs.d_vel, sizeof(float4) * vel.size(), cudaMemcpyDeviceToHost);
     const bool xs = m_bufs.xsphEnabled;
     if (!m_bufs.allocate(n) || !m_grid.allocate(n, m_grid.numCells)) return false;
+    m_bufs.allocateLists(m_listCapacity);
     m_bufs.xsphEnabled = xs;
     m_grid.hashed = m_useHashedGrid;
     cudaMemcpy(m_bufs.d_pos, pos.data(), sizeof(float4) * pos.size(), cudaMemcpyHostToDevice);
@@ -372,8 +405,29 @@ int Simulator::launchesPerStep() const {
     int n = 1 /*predict_keys*/ + 1 /*hist*/ + passes + 1 /*gather*/ + 1 /*lb*/;
     if (m_grid.hashed) n += 1;
     n += (m_params.solverIters > 0) ? 2 * m_params.solverIters : 1;
+    if (m_bufs.nbrListCap > 0) n += pbf::fused_list_builds(fused_shape(m_bufs, m_grid, m_params));
     n += 1; /*commit*/
     return n;
+}
+
+bool Simulator::setNeighbourListCapacity(uint32_t entries) {
+    if (m_stream) cudaStreamSynchronize(m_stream);
+    m_listCapacity = (entries + 7u) & ~7u;
+    m_graphDirty = true;
+    if (m_bufs.capacity == 0) return true;
+    return m_bufs.allocateLists(m_listCapacity);
+}
+
+bool Simulator::neighbourListStats(uint32_t& longest, uint32_t& overflowed, bool reset) {
+    longest = overflowed = 0;
+    if (!m_bufs.d_nbrStats) return m_bufs.nbrListCap == 0;
+    if (m_stream) cudaStreamSynchronize(m_stream);
+    uint32_t v[2] = {0, 0};
+    if (cudaMemcpy(v, m_bufs.d_nbrStats, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess) return false;
+    longest = v[0];
+    overflowed = v[1];
+    if (reset) cudaMemset(m_bufs.d_nbrStats, 0, sizeof(v));
+    return true;
 }
 
 int Simulator::profileStep(const SimParams& p, float* ms, const char** names, int cap) {
@@ -388,9 +442,10 @@ int Simulator::profileStep(const SimParams& p, float* ms, const char** names, in
     if (!uploadParamsIfChanged()) return -1;
     pbf::FusedBufs b = fused_bufs(m_bufs, m_grid);
     pbf::FusedShape sh = fused_shape(m_bufs, m_grid, m_params);
-    static const char* kIterNames[2][8] = {
+    static const char* kIterNames[3][8] = {
         {"lambda_1", "lambda_2", "lambda_3", "lambda_4", "lambda_5", "lambda_6", "lambda_7", "lambda_8"},
-        {"delta_1", "delta_2", "delta_3", "delta_4", "delta_5", "delta_6", "delta_7", "delta_8"}};
+        {"delta_1", "delta_2", "delta_3", "delta_4", "delta_5", "delta_6", "delta_7", "delta_8"},
+        {"lists_1", "lists_2", "lists_3", "lists_4", "lists_5", "lists_6", "lists_7", "lists_8"}};
     std::vector<cudaEvent_t> ev;
     std::vector<const char*> nm;
     auto mark = [&](const char* name) {
@@ -417,6 +472,7 @@ int Simulator::profileStep(const SimParams& p, float* ms, const char** names, in
         mark("finalize");
     } else {
         for (int it = 0; it < sh.iters; ++it) {
+            if (pbf::fused_build_lists(b, sh, it, m_stream) == cudaSuccess) mark(kIterNames[2][it]);
             pbf::fused_solve_phase(b, sh, it, 0, m_stream);
             mark(kIterNames[0][it]);
             pbf::fused_solve_phase(b, sh, it, 1, m_stream);

@@ -149,6 +149,8 @@ _SIGS = {
     "pbf_profile_step": ([_VP, C.POINTER(SimParams), C.POINTER(C.c_float), C.POINTER(C.c_char_p), _I,
                           C.POINTER(_I)], _I),
     "pbf_launches_per_step": ([_VP], _I),
+    "pbf_set_neighbour_list_capacity": ([_VP, _U32], _I),
+    "pbf_neighbour_list_stats": ([_VP, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32), _I], _I),
 }
 
 _ORACLE_SIGS = {
@@ -339,6 +341,16 @@ class Sim:
 
     def launches_per_step(self) -> int:
         return int(self.lib.pbf_launches_per_step(self.h))
+
+    def set_list_capacity(self, entries: int):
+        check(self.lib.pbf_set_neighbour_list_capacity(self.h, entries), "set_neighbour_list_capacity")
+
+    def list_stats(self, reset: bool = False):
+        """(capacity, longest list, overflowed lists) since the last reset."""
+        c, l, o = _U32(), _U32(), _U32()
+        check(self.lib.pbf_neighbour_list_stats(self.h, C.byref(c), C.byref(l), C.byref(o), int(reset)),
+              "neighbour_list_stats")
+        return int(c.value), int(l.value), int(o.value)
 
     def stream_ptr(self) -> int:
         return int(self.lib.pbf_stream(self.h) or 0)

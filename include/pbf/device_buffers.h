@@ -37,8 +37,18 @@ struct DeviceBuffers {
     double* d_stats = nullptr;         // 4 results + per-block partials
     uint32_t capacity = 0;
     bool xsphEnabled = false;  // XSPH post-op configured at initialize (sim/simulator.cpp:277-285)
+    // Neighbour lists of the GB300 step (cell order, nbrListCap entries per
+    // particle; nbrListCap = 0: no lists, every pass walks the stencil).
+    uint32_t* d_nbrList = nullptr;
+    uint32_t* d_nbrCount = nullptr;
+    uint32_t* d_nbrStats = nullptr;  // [0] longest list built, [1] overflowed lists
+    uint32_t nbrListCap = 0;
 
     bool allocate(uint32_t cap);
+    // (Re)allocates the lists for `capacity` particles; entries is rounded up
+    // to a multiple of 8.  On failure the lists are left off (returns false).
+    bool allocateLists(uint32_t entries);
+    void releaseLists();
     void release();
     ~DeviceBuffers() { release(); }
 };

@@ -235,6 +235,22 @@ int pbf_launches_per_step(pbf_sim* sim);
  * (PBF_ERR_TIMEOUT when a bounded wait gave up). */
 int pbf_synchronize(pbf_sim* sim);
 
+/* Neighbour lists.  No counterpart in the reference, whose solver passes
+ * each walk the whole 27-cell stencil.  Here the candidates within
+ * h + 2 * (position updates covered) * disp_clamp_max_h * h of each particle are
+ * listed once per step (once per span of solver iterations), in the stencil's
+ * order, and the lambda, delta and XSPH passes walk those lists; results are
+ * identical.  Lists are used only while the displacement clamp is on.
+ * entries = capacity per particle, rounded up to a multiple of 8 (default
+ * 512; 4 bytes of device memory per entry and particle); a particle with a
+ * longer list makes its warp walk the stencil.  0 turns lists off.  Takes
+ * effect at the next step. */
+int pbf_set_neighbour_list_capacity(pbf_sim* sim, uint32_t entries);
+/* *capacity = current capacity (0 = off); *longest = longest list built and
+ * *overflowed = lists longer than the capacity, both since the last reset
+ * (reset != 0 clears them after reading).  Any output may be NULL. */
+int pbf_neighbour_list_stats(pbf_sim* sim, uint32_t* capacity, uint32_t* longest, uint32_t* overflowed, int reset);
+
 /* Density-constraint diagnostics of the committed state, uncapped neighbour
  * sums over the step's cell grid: out[0] = mean |rho_i/rho0 - 1|,
  * out[1] = max |rho_i/rho0 - 1|, out[2] = mean max(rho_i/rho0 - 1, 0),

@@ -58,6 +58,7 @@ private:
     uint32_t m_numCells = 0;
     GridBounds m_grid{};
     bool m_xsph = false;
+    int m_listSpan = -1;
 };
 
 class Simulator {
@@ -110,6 +111,18 @@ public:
     // Kernel launches of this library per step for the current shape.
     int launchesPerStep() const;
 
+    // Neighbour lists (no counterpart in the reference).  Each solver pass
+    // of the GB300 step walks a per-particle list of the stencil candidates
+    // near it instead of the whole 27-cell stencil; results are identical.
+    // entries = list capacity per particle (rounded up to a multiple of 8;
+    // particles with more candidates walk the stencil); 0 turns lists off.
+    // Device memory: 4 * entries bytes per particle.
+    bool setNeighbourListCapacity(uint32_t entries);
+    uint32_t neighbourListCapacity() const { return m_bufs.nbrListCap; }
+    // Longest list built and number of overflowed lists since the last reset.
+    bool neighbourListStats(uint32_t& longest, uint32_t& overflowed, bool reset);
+    static constexpr uint32_t kDefaultListCapacity = 512;
+
 private:
     bool ensureCapacity(uint32_t n);
     bool uploadParamsIfChanged();
@@ -132,6 +145,7 @@ private:
     PhasePipeline m_pipeline;
     SimulationContext m_ctx;
     uint64_t m_frameIndex = 0;
+    uint32_t m_listCapacity = kDefaultListCapacity;
 };
 
 }  // namespace sim
