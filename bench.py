@@ -93,6 +93,15 @@ def alg_bytes_per_particle(phase: str, n: int, num_cells: int, hashed: bool, ite
     return 0.0
 
 
+def issue_peak(clk) -> float:
+    """Warp instructions per second the GPU can issue: 4 schedulers per SM."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    return 4.0 * sms * mhz * 1e6
+
+
 def step_alg_bytes(num_cells: int, iters: int) -> float:
     """Whole-step compulsory bytes: 202 + 16 P + 60 iters per particle."""
     passes = (key_bits(num_cells) + 7) // 8
@@ -299,7 +308,7 @@ def run_ours(args, cfg, world, rank, local):
 
     # Live per-phase profile (after the timed region): dominant kernel.
     prof = {}
-    for _ in range(args.profile_steps):
+    for _ in range(max(1, args.profile_steps)):
         for name, ms in sim.profile_step():
             prof.setdefault(name, []).append(ms)
     avg = {k: sum(v) / len(v) for k, v in prof.items()}
@@ -307,13 +316,18 @@ def run_ours(args, cfg, world, rank, local):
     dom = max(avg, key=avg.get)
     dom_bytes = alg_bytes_per_particle(dom, n, nc, hashed, cfg["iters"]) * n
     achieved = dom_bytes / (avg[dom] * 1e-3) / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic_c2.json")
+    # DRAM traffic and warp instructions per launch of the dominant kernel, from
+    # the committed ncu capture of the same workload.
+    traffic = inst = None
+    tfile = os.path.join(ROOT, "profiles", "c2_dram_traffic.txt")
     if cfg is CONFIGS["c2"] and os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(dom.split("_")[0] if dom[-1].isdigit() else dom)
+        rows = {ln.split()[0]: ln.split()[1:] for ln in open(tfile) if ln.strip() and not ln.startswith("#")}
+        rec = rows.get(dom.split("_")[0])
+        if rec:
+            traffic, inst = int(rec[0]), int(rec[1])
 
     # End to end through host buffers.
-    e2e_steps = min(args.steps, args.e2e_steps)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
     hp = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
     hv = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
     pbfx.check(lib.pbf_download_state(sim.h, C.c_void_p(hp.data_ptr()), C.c_void_p(hv.data_ptr())))
@@ -342,6 +356,13 @@ def run_ours(args, cfg, world, rank, local):
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": dom_bytes, "ms_per_launch": avg[dom],
                      "share_of_step": avg[dom] / total_phase},
+        "issue_roofline": None if inst is None else {
+            "kernel": dom, "unit": "warp-instructions/s", "warp_instructions_per_launch": inst,
+            "achieved": inst / (avg[dom] * 1e-3), "peak": issue_peak(clk),
+            "frac": inst / (avg[dom] * 1e-3) / issue_peak(clk),
+            "note": "the neighbour passes are bound by FP32 issue, not HBM: instructions per launch from "
+                    "profiles/c2_dram_traffic.txt (ncu), time live; peak = 4 warp-instructions per cycle "
+                    "per SM x SMs x sampled SM clock"},
         "step_roofline": {"alg_bytes_per_particle_step": step_alg_bytes(nc, cfg["iters"]),
                           "achieved": value * step_alg_bytes(nc, cfg["iters"]) / 1e9, "peak": hbm_peak,
                           "unit": "GB/s",

@@ -324,7 +324,7 @@ __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E
                 const bool v = !done && e + uint32_t(u) < n;
                 const uint32_t k = v ? ks[u] : src.fill;
                 const bool h = v && hit(k);
-                q[cnt * kStride] = QT(k);  // cnt <= Q - 1 here: the queue holds <= Q - kChunk at a chunk's start
+                q[cnt * kStride] = QT(k);  // cnt <= Q - 1 here: at most Q - kChunk queued at a chunk's start
                 cnt += h ? 1 : 0;
                 total += h ? 1 : 0;
                 done = done || total >= maxHits;
