@@ -52,6 +52,10 @@ CONFIGS = {
                workload="dam_break_1M_2iter_hashed (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
     "c2_dense": dict(box=(2.0, 1.0, 2.0), lattice=(128, 64, 128), iters=2, hashed=False,
                      workload="dam_break_1M_2iter_dense (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
+    # batched ensemble: 256 seeded scenes (pbfx.ensemble_scenes)
+    "c4": dict(scenes=256, seed=0xE45E, iters=3, hashed=True,
+               workload="ensemble_256_scenes (N_s log-uniform in [2048, 65536], boxes U[0.3,1]^3 m, gravity tilted "
+                        "<= 15 deg, 2 or 3 iterations, seed 0xE45E)"),
 }
 
 METRIC = "particle-steps/s @1M"
@@ -402,6 +406,141 @@ def run_ours(args, cfg, world, rank, local):
     return 0
 
 
+def run_ensemble(args, cfg, world, rank, local):
+    """C4: the batched ensemble vs the same scenes stepped one by one."""
+    import torch
+
+    import __graft_entry__ as g
+    import pbfx
+
+    if rank == 0 or world == 1:
+        g.build_library()
+        g.build_oracle()
+    barrier(world)
+    torch.cuda.set_device(local)
+    lib = pbfx.load()
+    scenes, pos = pbfx.ensemble_scenes(lib, cfg["scenes"], seed=cfg["seed"])
+    vel = np.zeros_like(pos)
+    S, n = len(scenes), pos.shape[0]
+    ens = pbfx.Ensemble(lib, scenes)
+    ens.upload(pos, vel)
+    stream = torch.cuda.ExternalStream(ens.stream_ptr())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    pbfx.check(lib.pbf_ensemble_step(ens.h, args.warmup))
+    pbfx.check(lib.pbf_ensemble_synchronize(ens.h))
+    snap_pos, snap_vel = ens.download()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush, outside the timed window
+            ev[k][0].record(stream)
+            lib.pbf_ensemble_step(ens.h, 1)
+            ev[k][1].record(stream)
+    pbfx.check(lib.pbf_ensemble_synchronize(ens.h))
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop(None)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s, units = aggregate(sum(step_ms) / 1e3, float(S) * args.steps, world)
+    value = units / total_s
+
+    # End to end: host state in and out every step.
+    hp = torch.from_numpy(snap_pos.copy()).pin_memory()
+    hv = torch.from_numpy(snap_vel.copy()).pin_memory()
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        pbfx.check(lib.pbf_ensemble_step_host(ens.h, C.c_void_p(hp.data_ptr()), C.c_void_p(hv.data_ptr())))
+    e2e_s = time.perf_counter() - t0
+    launches = ens.launches_per_step() * args.steps
+    ens.close()
+
+    # Looped: every scene its own pbf_sim, stepped scene after scene from the
+    # same post-warm-up state (each handle on its own stream, so neighbouring
+    # scenes' launches may overlap on the GPU).
+    loop_steps = max(1, min(args.steps, args.loop_steps))
+    off = np.zeros(S + 1, np.int64)
+    off[1:] = np.cumsum([p.numParticles for p in scenes])
+    sims = []
+    for k, p in enumerate(scenes):
+        sm = pbfx.Sim(lib, p, hashed=True)
+        sm.upload(snap_pos[off[k]:off[k + 1]], snap_vel[off[k]:off[k + 1]])
+        sims.append(sm)
+    for sm in sims:  # graph capture and upload, outside the timing
+        pbfx.check(lib.pbf_step(sm.h, None))
+    torch.cuda.synchronize()
+    for k, sm in enumerate(sims):
+        sm.upload(snap_pos[off[k]:off[k + 1]], snap_vel[off[k]:off[k + 1]])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(loop_steps):
+        for sm in sims:
+            lib.pbf_step(sm.h, None)
+    for sm in sims:
+        pbfx.check(lib.pbf_synchronize(sm.h))
+    loop_s = time.perf_counter() - t0
+    for sm in sims:
+        sm.close()
+    looped = S * loop_steps / loop_s
+
+    line = {
+        "metric": "scene-steps/s (ensemble of 256 scenes)", "value": value, "unit": "scene-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (pbfx.ensemble_scenes, seed 0x%X)" % cfg["seed"],
+        "config": {"workload": cfg["workload"], "scenes": S, "particles": n,
+                   "particles_per_scene": [int(min(p.numParticles for p in scenes)),
+                                           int(max(p.numParticles for p in scenes))],
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "timed_steps": "steps %d..%d of the run from the seeded lattices" % (
+                       args.warmup, args.warmup + args.steps - 1),
+                   "l2": "flushed before every timed step (256 MiB write, untimed)"},
+        "particle_steps_per_s": n * args.steps / total_s,
+        "looped": {"value": looped, "unit": "scene-steps/s", "steps": loop_steps,
+                   "what": "each scene its own pbf_sim (fused step, one graph per scene-step), host loop over "
+                           "scenes, same post-warm-up state, wall clock",
+                   "speedup_of_ensemble": value / looped},
+        "e2e": {"value": S * e2e_steps / e2e_s, "unit": "scene-steps/s", "h2d_bytes_per_step": 32 * n,
+                "d2h_bytes_per_step": 32 * n, "steps": e2e_steps,
+                "api": "pbf_ensemble_step_host (pinned host pos/vel in, one step, pos/vel out)"},
+        "step_ms": {"first": round(step_ms[0], 4), "median": round(statistics.median(step_ms), 4),
+                    "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+
+    # The reference's own kernels looped scene by scene (graph per step).
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        ref = pbfx.load_ref()
+        if ref is not None:
+            total_ms = 0.0
+            ok = True
+            for k, p in enumerate(scenes):
+                rp = np.ascontiguousarray(snap_pos[off[k]:off[k + 1]])
+                rv = np.ascontiguousarray(snap_vel[off[k]:off[k + 1]])
+                ms = C.c_double()
+                if ref.ref_time_steps(C.byref(p), 1, pbfx.ptr(rp), pbfx.ptr(rv), int(p.numParticles), 0,
+                                      loop_steps, C.byref(ms)) != 0:
+                    ok = False
+                    break
+                total_ms += ms.value * loop_steps
+            if ok:
+                line["reference_gpu_looped"] = {
+                    "value": S * loop_steps / (total_ms * 1e-3), "unit": "scene-steps/s",
+                    "what": "reference kernels (sim/*.cu) built for sm_103a, each scene stepped alone, device time "
+                            "of its graphs summed over scenes (launch gaps between scenes not counted)",
+                    "speedup_of_ensemble": value / (S * loop_steps / (total_ms * 1e-3))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -415,13 +554,20 @@ def main(argv=None):
     ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--loop-steps", type=int, default=10, help="steps of the looped baseline (c4)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world, rank, local = dist_setup()
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
+        if "scenes" in cfg:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched ensemble; "
+                              "bench.py --config c4 reports its looped kernels as reference_gpu_looped"}))
+            return 0
         return run_reference(args, cfg, world, rank)
+    if "scenes" in cfg:
+        return run_ensemble(args, cfg, world, rank, local)
     return run_ours(args, cfg, world, rank, local)
 
 

@@ -1,0 +1,392 @@
+// ensemble.cu - many independent scenes stepped as one workload.
+//
+// The reference steps one scene per sim::Simulator (sim/simulator.cpp:560-643);
+// a batch of scenes is a loop over simulators, each step a dozen small launches
+// that leave most of the GPU idle for scenes of a few thousand particles.  Here
+// the scenes' particles are concatenated (scene s owns ids [off[s], off[s+1]))
+// and every phase is one launch over all of them:
+//   * cell keys are global: scene s's cells are numbered from cellOff[s], so a
+//     single stable sort of the keys orders particles by (scene, cell, id), the
+//     order each scene's own sort produces, and one lower-bound table over all
+//     scenes' cells gives every scene its cell ranges;
+//   * each particle reads its scene's parameter block (grid, gravity, dt,
+//     kernel, tuning, iteration count); a warp may hold particles of two
+//     scenes, which the per-lane walks allow;
+//   * scenes with fewer solver iterations than the ensemble's maximum carry
+//     their prediction through the remaining passes unchanged.
+// Every scene therefore evolves bit-identically to a pbf_sim of the same
+// parameters.  The step is one CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/pbf/pbf.h"
+#include "grid.cuh"
+#include "pbf_common.cuh"
+#include "sort.cuh"
+
+namespace pbf {
+namespace {
+
+constexpr int kBS = 256;
+constexpr int kEnsBS = 128;
+constexpr int kEnsQueue = 32;
+
+struct SceneInfo {
+    sim::DeviceParams dp;
+    uint32_t cellOffset;
+    int iters;
+};
+
+__global__ void __launch_bounds__(kBS) k_ens_predict_keys(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                          const SceneInfo* __restrict__ scenes,
+                                                          const uint32_t* __restrict__ sceneOfId, uint32_t N,
+                                                          uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const SceneInfo& sc = scenes[sceneOfId[i]];
+    const float4 x = predict_clamped(pos[i], vel[i], sc.dp.gravity, sc.dp.dt, sc.dp.grid);
+    keys[i] = sc.cellOffset + cell_key(x, sc.dp.grid);
+}
+
+__global__ void __launch_bounds__(kBS) k_ens_gather(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
+                                                    const float4* __restrict__ vel,
+                                                    const SceneInfo* __restrict__ scenes,
+                                                    const uint32_t* __restrict__ sceneOfId, uint32_t N,
+                                                    float4* __restrict__ pred_s, float4* __restrict__ pos_s,
+                                                    uint32_t* __restrict__ sceneOfSlot) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const uint32_t i = perm[s];
+    const uint32_t sc = sceneOfId[i];
+    const float4 p = pos[i];
+    pred_s[s] = predict_clamped(p, vel[i], scenes[sc].dp.gravity, scenes[sc].dp.dt, scenes[sc].dp.grid);
+    pos_s[s] = p;
+    sceneOfSlot[s] = sc;
+}
+
+// Stencil rows of slot s in its scene's cell range.
+__device__ __forceinline__ RowSource scene_rows(const SceneInfo& sc, uint32_t key, const uint32_t* __restrict__ lb) {
+    RowSource r;
+    decode_key(key - sc.cellOffset, sc.dp.grid.dim, r.cx, r.cy, r.cz);
+    r.reach = neighbour_reach(sc.dp);
+    r.dim = sc.dp.grid.dim;
+    r.lb = lb + sc.cellOffset;
+    return r;
+}
+
+__global__ void __launch_bounds__(kEnsBS) k_ens_lambda(int it, const float4* __restrict__ pred,
+                                                       const uint32_t* __restrict__ key_s,
+                                                       const uint32_t* __restrict__ lb,
+                                                       const SceneInfo* __restrict__ scenes,
+                                                       const uint32_t* __restrict__ sceneOfSlot, uint32_t N,
+                                                       float* __restrict__ lam) {
+    __shared__ uint32_t s_queue[kEnsQueue * kEnsBS];
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t sc = s < N ? s : 0u;
+    const SceneInfo& scene = scenes[sceneOfSlot[sc]];
+    const bool active = s < N && it < scene.iters;  // every lane takes part in the warp-wide rounds
+    const float l = lambda_queued<kEnsQueue, kEnsBS>(active, sc, pred[sc], scene_rows(scene, key_s[sc], lb), scene.dp,
+                                                     GlobalData{pred, nullptr, nullptr}, s_queue + threadIdx.x);
+    if (active) lam[s] = l;
+}
+
+__global__ void __launch_bounds__(kEnsBS) k_ens_delta(int it, const float4* __restrict__ pred,
+                                                      const float* __restrict__ lam,
+                                                      const uint32_t* __restrict__ key_s,
+                                                      const uint32_t* __restrict__ lb,
+                                                      const SceneInfo* __restrict__ scenes,
+                                                      const uint32_t* __restrict__ sceneOfSlot, uint32_t N,
+                                                      float4* __restrict__ pred_out,
+                                                      const float4* __restrict__ pos_s, float4* __restrict__ vel_s) {
+    __shared__ uint32_t s_queue[kEnsQueue * kEnsBS];
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t sc = s < N ? s : 0u;
+    const SceneInfo& scene = scenes[sceneOfSlot[sc]];
+    const sim::DeviceParams& dp = scene.dp;
+    const bool solve = s < N && it < scene.iters;
+    const float4 pi = pred[sc];
+    const float3 d = delta_queued<kEnsQueue, kEnsBS>(solve, sc, pi, lam[sc], scene_rows(scene, key_s[sc], lb), dp,
+                                                     scorr_wq(dp), GlobalData{pred, lam, nullptr},
+                                                     s_queue + threadIdx.x);
+    if (s >= N) return;
+    // A scene past its iterations carries its prediction through; a scene
+    // without iterations applies boundary and velocity to it in pass 0.
+    const bool last = solve ? it == scene.iters - 1 : (scene.iters <= 0 && it == 0);
+    float4 x = solve ? make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w) : pi;
+    if (last) {
+        // Boundary(e=0) after the solve loop (sim/phases.cpp:94) and the
+        // velocity phase (sim/phases.cpp:102-105).
+        float4 vdummy = make_float4(0.f, 0.f, 0.f, 0.f);
+        boundary_apply(x, vdummy, dp.grid, 0.0f);
+        const float inv_dt = div_(1.0f, dp.dt);
+        const float4 p = pos_s[s];
+        vel_s[s] = make_float4(mul_(sub_(x.x, p.x), inv_dt), mul_(sub_(x.y, p.y), inv_dt),
+                               mul_(sub_(x.z, p.z), inv_dt), 0.0f);
+    }
+    pred_out[s] = x;
+}
+
+__global__ void __launch_bounds__(kEnsBS) k_ens_commit(const float4* __restrict__ pred,
+                                                       const float4* __restrict__ vel_s,
+                                                       const uint32_t* __restrict__ key_s,
+                                                       const uint32_t* __restrict__ lb,
+                                                       const uint32_t* __restrict__ perm,
+                                                       const SceneInfo* __restrict__ scenes,
+                                                       const uint32_t* __restrict__ sceneOfSlot, uint32_t N,
+                                                       float4* __restrict__ pos, float4* __restrict__ vel) {
+    __shared__ uint32_t s_queue[kEnsQueue * kEnsBS];
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t sc = s < N ? s : 0u;
+    const SceneInfo& scene = scenes[sceneOfSlot[sc]];
+    const sim::DeviceParams& dp = scene.dp;
+    float4 x = pred[sc];
+    float4 v = vel_s[sc];
+    // XSPH where the scene configures it (sim/simulator.cpp:277-285)
+    const bool xsph = s < N && dp.xsph_c > 0.f;
+    const float4 vx = xsph_queued<kEnsQueue, kEnsBS>(xsph, sc, x, v, scene_rows(scene, key_s[sc], lb), dp,
+                                                     GlobalData{pred, nullptr, vel_s}, s_queue + threadIdx.x);
+    if (s >= N) return;
+    if (xsph) v = vx;
+    boundary_apply(x, v, dp.grid, dp.boundaryRestitution);
+    const uint32_t i = perm[s];
+    pos[i] = x;
+    vel[i] = v;
+}
+
+template <class T>
+bool dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count) == cudaSuccess;
+}
+
+int from_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return PBF_OK;
+    if (e == cudaErrorMemoryAllocation) return PBF_ERR_OOM;
+    return PBF_ERR_CUDA;
+}
+
+int3 dims_of(const sim::GridBounds& g) {
+    const float cs = (g.cellSize > 0.f) ? g.cellSize : 1.f;
+    int3 d;
+    d.x = std::max(0, int(ceilf((g.maxs.x - g.mins.x) / cs)));
+    d.y = std::max(0, int(ceilf((g.maxs.y - g.mins.y) / cs)));
+    d.z = std::max(0, int(ceilf((g.maxs.z - g.mins.z) / cs)));
+    return d;
+}
+
+}  // namespace
+}  // namespace pbf
+
+struct pbf_ensemble {
+    cudaStream_t stream = nullptr;
+    uint32_t N = 0, S = 0, totalCells = 0;
+    int keyBits = 1, passes = 1;
+    std::vector<uint32_t> offsets;
+    float4 *pos = nullptr, *vel = nullptr, *pred_a = nullptr, *pred_b = nullptr, *pos_s = nullptr, *vel_s = nullptr;
+    float* lam = nullptr;
+    uint32_t *keys = nullptr, *key_s = nullptr, *perm = nullptr, *lb = nullptr, *sceneOfId = nullptr,
+             *sceneOfSlot = nullptr, *err = nullptr;
+    pbf::SceneInfo* scenes = nullptr;
+    void* sortTemp = nullptr;
+    size_t sortBytes = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    ~pbf_ensemble() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (void* p : {(void*)pos, (void*)vel, (void*)pred_a, (void*)pred_b, (void*)pos_s, (void*)vel_s, (void*)lam,
+                        (void*)keys, (void*)key_s, (void*)perm, (void*)lb, (void*)sceneOfId, (void*)sceneOfSlot,
+                        (void*)err, (void*)scenes, sortTemp})
+            if (p) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    float4* final_pred() const { return (passes % 2 == 0) ? pred_a : pred_b; }
+
+    // The step as launches on `stream` (captured once into the graph).
+    cudaError_t enqueue() {
+        using namespace pbf;
+        if (N == 0) return cudaSuccess;
+        const unsigned g = blocks_for(N, kBS), gn = blocks_for(N, kEnsBS);
+        k_ens_predict_keys<<<g, kBS, 0, stream>>>(pos, vel, scenes, sceneOfId, N, keys);
+        cudaError_t e = sort_pairs(sortTemp, sortBytes, keys, key_s, nullptr, perm, N, keyBits, stream, err);
+        if (e != cudaSuccess) return e;
+        k_ens_gather<<<g, kBS, 0, stream>>>(perm, pos, vel, scenes, sceneOfId, N, pred_a, pos_s, sceneOfSlot);
+        if ((e = launch_cell_lb(lb, key_s, N, totalCells, stream)) != cudaSuccess) return e;
+        for (int it = 0; it < passes; ++it) {
+            float4* cur = (it % 2 == 0) ? pred_a : pred_b;
+            float4* nxt = (it % 2 == 0) ? pred_b : pred_a;
+            k_ens_lambda<<<gn, kEnsBS, 0, stream>>>(it, cur, key_s, lb, scenes, sceneOfSlot, N, lam);
+            k_ens_delta<<<gn, kEnsBS, 0, stream>>>(it, cur, lam, key_s, lb, scenes, sceneOfSlot, N, nxt, pos_s,
+                                                   vel_s);
+        }
+        k_ens_commit<<<gn, kEnsBS, 0, stream>>>(final_pred(), vel_s, key_s, lb, perm, scenes, sceneOfSlot, N, pos,
+                                                vel);
+        return cudaGetLastError();
+    }
+
+    int capture() {
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBF_ERR_CUDA;
+        const cudaError_t le = enqueue();
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(stream, &gr);
+        if (le != cudaSuccess || ce != cudaSuccess || !gr) {
+            if (gr) cudaGraphDestroy(gr);
+            cudaGetLastError();
+            return PBF_ERR_CUDA;
+        }
+        if (cudaGraphInstantiate(&exec, gr, 0) != cudaSuccess) {
+            cudaGraphDestroy(gr);
+            exec = nullptr;
+            return PBF_ERR_CUDA;
+        }
+        graph = gr;
+        return pbf::from_cuda(cudaGraphUpload(exec, stream));
+    }
+};
+
+extern "C" {
+
+int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_ensemble** out) {
+    using namespace pbf;
+    if (!out) return PBF_ERR_INVALID;
+    *out = nullptr;
+    if (!params || num_scenes == 0) return PBF_ERR_INVALID;
+    const sim::SimParams* sp = reinterpret_cast<const sim::SimParams*>(params);
+    std::vector<SceneInfo> info(num_scenes);
+    std::vector<uint32_t> offsets(num_scenes + 1, 0);
+    uint64_t n = 0, cells = 0;
+    int passes = 0;
+    for (uint32_t s = 0; s < num_scenes; ++s) {
+        sim::SimParams p = sp[s];
+        if (p.solverIters < 0 || !(p.grid.cellSize > 0.f)) return PBF_ERR_INVALID;
+        p.grid.dim = dims_of(p.grid);
+        const uint64_t nc = uint64_t(p.grid.dim.x) * uint64_t(p.grid.dim.y) * uint64_t(p.grid.dim.z);
+        if (nc == 0) return PBF_ERR_INVALID;
+        std::memset(&info[s], 0, sizeof(SceneInfo));
+        info[s].dp = sim::MakeDeviceParams(p);
+        info[s].cellOffset = uint32_t(cells);
+        info[s].iters = p.solverIters;
+        offsets[s] = uint32_t(n);
+        n += p.numParticles;
+        cells += nc;
+        passes = std::max(passes, p.solverIters);
+        if (n > 0xFFFFFFF0ull || cells > 0xFFFFFFF0ull) return PBF_ERR_UNSUPPORTED;
+    }
+    offsets[num_scenes] = uint32_t(n);
+    pbf_ensemble* e = new (std::nothrow) pbf_ensemble;
+    if (!e) return PBF_ERR_OOM;
+    e->N = uint32_t(n);
+    e->S = num_scenes;
+    e->totalCells = uint32_t(cells);
+    e->keyBits = bits_for(e->totalCells - 1u);
+    e->passes = std::max(1, passes);
+    e->offsets = offsets;
+    e->sortBytes = sort_temp_bytes(e->N, e->keyBits);
+    std::vector<uint32_t> sceneOfId(e->N);
+    for (uint32_t s = 0; s < num_scenes; ++s)
+        std::fill(sceneOfId.begin() + offsets[s], sceneOfId.begin() + offsets[s + 1], s);
+    const uint32_t N = e->N;
+    bool ok = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess && dalloc(&e->pos, N) &&
+              dalloc(&e->vel, N) && dalloc(&e->pred_a, N) && dalloc(&e->pred_b, N) && dalloc(&e->pos_s, N) &&
+              dalloc(&e->vel_s, N) && dalloc(&e->lam, N) && dalloc(&e->keys, N) && dalloc(&e->key_s, N) &&
+              dalloc(&e->perm, N) && dalloc(&e->lb, size_t(e->totalCells) + 1) && dalloc(&e->sceneOfId, N) &&
+              dalloc(&e->sceneOfSlot, N) && dalloc(&e->err, 1) && dalloc(&e->scenes, num_scenes) &&
+              cudaMalloc(&e->sortTemp, e->sortBytes) == cudaSuccess;
+    if (ok) {
+        ok = cudaMemcpy(e->scenes, info.data(), sizeof(SceneInfo) * num_scenes, cudaMemcpyHostToDevice) ==
+                 cudaSuccess &&
+             cudaMemcpy(e->sceneOfId, sceneOfId.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice) ==
+                 cudaSuccess &&
+             cudaMemset(e->pos, 0, sizeof(float4) * std::max<uint32_t>(N, 1)) == cudaSuccess &&
+             cudaMemset(e->vel, 0, sizeof(float4) * std::max<uint32_t>(N, 1)) == cudaSuccess &&
+             cudaMemset(e->err, 0, sizeof(uint32_t)) == cudaSuccess;
+    }
+    if (!ok) {
+        const cudaError_t ce = cudaGetLastError();
+        delete e;
+        return ce == cudaErrorMemoryAllocation ? PBF_ERR_OOM : PBF_ERR_CUDA;
+    }
+    const int st = e->capture();
+    if (st != PBF_OK) {
+        delete e;
+        return st;
+    }
+    *out = e;
+    return PBF_OK;
+}
+
+int pbf_ensemble_destroy(pbf_ensemble* e) {
+    delete e;
+    return PBF_OK;
+}
+
+void* pbf_ensemble_stream(pbf_ensemble* e) { return e ? static_cast<void*>(e->stream) : nullptr; }
+
+uint32_t pbf_ensemble_num_particles(pbf_ensemble* e) { return e ? e->N : 0u; }
+
+int pbf_ensemble_scene_offsets(pbf_ensemble* e, uint32_t* offsets) {
+    if (!e || !offsets) return PBF_ERR_INVALID;
+    std::memcpy(offsets, e->offsets.data(), sizeof(uint32_t) * e->offsets.size());
+    return PBF_OK;
+}
+
+int pbf_ensemble_upload_state(pbf_ensemble* e, const float4* pos, const float4* vel) {
+    if (!e || !pos || !vel) return PBF_ERR_INVALID;
+    const size_t bytes = sizeof(float4) * e->N;
+    cudaMemcpyAsync(e->pos, pos, bytes, cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->vel, vel, bytes, cudaMemcpyHostToDevice, e->stream);
+    return pbf::from_cuda(cudaStreamSynchronize(e->stream));
+}
+
+int pbf_ensemble_download_state(pbf_ensemble* e, float4* pos, float4* vel) {
+    if (!e) return PBF_ERR_INVALID;
+    const size_t bytes = sizeof(float4) * e->N;
+    if (pos) cudaMemcpyAsync(pos, e->pos, bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (vel) cudaMemcpyAsync(vel, e->vel, bytes, cudaMemcpyDeviceToHost, e->stream);
+    return pbf::from_cuda(cudaStreamSynchronize(e->stream));
+}
+
+int pbf_ensemble_step(pbf_ensemble* e, int n) {
+    if (!e || n < 0) return PBF_ERR_INVALID;
+    for (int i = 0; i < n; ++i)
+        if (cudaGraphLaunch(e->exec, e->stream) != cudaSuccess) return PBF_ERR_CUDA;
+    return PBF_OK;
+}
+
+int pbf_ensemble_step_host(pbf_ensemble* e, float4* pos, float4* vel) {
+    if (!e || !pos || !vel) return PBF_ERR_INVALID;
+    const size_t bytes = sizeof(float4) * e->N;
+    cudaMemcpyAsync(e->pos, pos, bytes, cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->vel, vel, bytes, cudaMemcpyHostToDevice, e->stream);
+    if (cudaGraphLaunch(e->exec, e->stream) != cudaSuccess) return PBF_ERR_CUDA;
+    cudaMemcpyAsync(pos, e->pos, bytes, cudaMemcpyDeviceToHost, e->stream);
+    cudaMemcpyAsync(vel, e->vel, bytes, cudaMemcpyDeviceToHost, e->stream);
+    return pbf::from_cuda(cudaStreamSynchronize(e->stream));
+}
+
+int pbf_ensemble_synchronize(pbf_ensemble* e) {
+    if (!e) return PBF_ERR_INVALID;
+    const cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return pbf::from_cuda(ce);
+    uint32_t err = 0;
+    if (cudaMemcpy(&err, e->err, sizeof(err), cudaMemcpyDeviceToHost) != cudaSuccess) return PBF_ERR_CUDA;
+    if (err) {
+        cudaMemset(e->err, 0, sizeof(uint32_t));
+        return (err & pbf::kErrLookbackTimeoutBit) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
+    }
+    return PBF_OK;
+}
+
+int pbf_ensemble_launches_per_step(pbf_ensemble* e) {
+    if (!e) return 0;
+    const int sortPasses = (e->keyBits + 7) / 8;
+    return 1 /*predict_keys*/ + 1 /*hist*/ + sortPasses + 1 /*gather*/ + 1 /*lb*/ + 2 * e->passes + 1 /*commit*/;
+}
+
+}  // extern "C"

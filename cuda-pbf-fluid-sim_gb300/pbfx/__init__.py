@@ -7,6 +7,7 @@ fails loudly when it has not been built (there is no fallback path).
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -150,6 +151,17 @@ _SIGS = {
                           C.POINTER(_I)], _I),
     "pbf_launches_per_step": ([_VP], _I),
     "pbf_set_neighbour_list_capacity": ([_VP, _U32], _I),
+    "pbf_ensemble_create": ([C.POINTER(SimParams), _U32, C.POINTER(_VP)], _I),
+    "pbf_ensemble_destroy": ([_VP], _I),
+    "pbf_ensemble_stream": ([_VP], _VP),
+    "pbf_ensemble_num_particles": ([_VP], _U32),
+    "pbf_ensemble_scene_offsets": ([_VP, _VP], _I),
+    "pbf_ensemble_upload_state": ([_VP, _VP, _VP], _I),
+    "pbf_ensemble_download_state": ([_VP, _VP, _VP], _I),
+    "pbf_ensemble_step": ([_VP, _I], _I),
+    "pbf_ensemble_step_host": ([_VP, _VP, _VP], _I),
+    "pbf_ensemble_synchronize": ([_VP], _I),
+    "pbf_ensemble_launches_per_step": ([_VP], _I),
     "pbf_neighbour_list_stats": ([_VP, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32), _I], _I),
 }
 
@@ -359,6 +371,104 @@ class Sim:
         out = (C.c_double * 4)()
         check(self.lib.pbf_density_stats(self.h, C.byref(out)), "density_stats")
         return list(out)
+
+
+class Ensemble:
+    """Owning wrapper of a pbf_ensemble handle (scenes: a list of SimParams)."""
+
+    def __init__(self, lib, scenes):
+        self.lib = lib
+        arr = (SimParams * len(scenes))(*scenes)
+        self.h = C.c_void_p()
+        check(lib.pbf_ensemble_create(arr, len(scenes), C.byref(self.h)), "pbf_ensemble_create")
+        self.n = int(lib.pbf_ensemble_num_particles(self.h))
+        self.offsets = np.zeros(len(scenes) + 1, np.uint32)
+        check(lib.pbf_ensemble_scene_offsets(self.h, ptr(self.offsets)), "scene_offsets")
+
+    def close(self):
+        if self.h:
+            self.lib.pbf_ensemble_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, pos: np.ndarray, vel: np.ndarray):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        assert pos.shape == (self.n, 4) and vel.shape == (self.n, 4)
+        check(self.lib.pbf_ensemble_upload_state(self.h, ptr(pos), ptr(vel)), "ensemble upload")
+
+    def download(self):
+        pos = np.zeros((self.n, 4), np.float32)
+        vel = np.zeros((self.n, 4), np.float32)
+        check(self.lib.pbf_ensemble_download_state(self.h, ptr(pos), ptr(vel)), "ensemble download")
+        return pos, vel
+
+    def step(self, n: int = 1):
+        check(self.lib.pbf_ensemble_step(self.h, n), "ensemble step")
+        check(self.lib.pbf_ensemble_synchronize(self.h), "ensemble synchronize")
+
+    def stream_ptr(self) -> int:
+        return int(self.lib.pbf_ensemble_stream(self.h) or 0)
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.pbf_ensemble_launches_per_step(self.h))
+
+
+def lattice_dims(total: int, box_extent, spacing: float):
+    """Lattice (nx, ny, nz) holding `total` particles packed from the min
+    corner of a box, as Simulator::seedBoxLatticeAuto chooses it
+    (sim/simulator.cpp:880-934)."""
+    cap = [max(1, int(math.floor(e / spacing))) for e in box_extent]
+    t = max(1, total)
+    nx = min(cap[0], int(math.ceil(t ** (1.0 / 3.0))))
+    rem = (t + nx - 1) // nx
+    ny = min(cap[1], int(math.ceil(math.sqrt(rem))))
+    nz = min(cap[2], int(math.ceil(rem / max(1, ny))))
+    while nx * ny * nz < t:
+        if nx < cap[0]:
+            nx += 1
+        elif ny < cap[1]:
+            ny += 1
+        elif nz < cap[2]:
+            nz += 1
+        else:
+            break
+    return nx, ny, nz
+
+
+def ensemble_scenes(lib, num_scenes: int, seed: int = 0xE45E, n_min: int = 2048, n_max: int = 65536,
+                    iters_choices=(2, 3)):
+    """Seeded batch of dam-break scenes: N_s = round(exp(U[ln n_min, ln n_max])),
+    box extents U[0.3, 1.0]^3 m, gravity 9.8 m/s^2 tilted from -y by up to 15
+    degrees in a uniform direction, solver iterations drawn from iters_choices,
+    a block of N_s lattice particles at spacing 0.01 (jitter +-0.0005) packed
+    from the box's min corner (a box that cannot hold N_s particles at that
+    spacing is filled: fewer particles).  Returns (list of SimParams,
+    concatenated pos)."""
+    rng = np.random.default_rng(seed)
+    scenes, blocks = [], []
+    for s in range(num_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        ext = rng.uniform(0.3, 1.0, 3)
+        iters = int(rng.choice(iters_choices))
+        p = dam_break_params(tuple(float(e) for e in ext), iters, n)
+        theta = math.radians(rng.uniform(0.0, 15.0))
+        phi = rng.uniform(0.0, 2.0 * math.pi)
+        g = 9.8
+        p.gravity = Float3(g * math.sin(theta) * math.cos(phi), -g * math.cos(theta), g * math.sin(theta) * math.sin(phi))
+        nx, ny, nz = lattice_dims(n, ext, 0.01)
+        # a box too small for N_s particles at this spacing is filled instead
+        n = min(n, nx * ny * nz)
+        pos = seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, seed * 1000003 + s, p)[:n]
+        p.numParticles = p.maxParticles = n
+        scenes.append(p)
+        blocks.append(pos)
+    return scenes, np.ascontiguousarray(np.concatenate(blocks))
 
 
 def oracle_step(orc, params: SimParams, hashed: bool, pos: np.ndarray, vel: np.ndarray, trace: bool = True):

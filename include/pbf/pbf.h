@@ -272,6 +272,33 @@ enum {
 };
 int pbf_debug_fetch(pbf_sim* sim, int item, void* host_dst, size_t bytes);
 
+/* --------------------------------------------------------- batched ensemble */
+/* Many independent scenes stepped as one workload.  No counterpart in the
+ * reference, which steps one scene per sim::Simulator (sim/simulator.cpp:
+ * 560-643), so a batch there is a loop over simulators.  scenes[s] holds scene
+ * s's parameters (numParticles, grid box and cell size, gravity, dt, kernel,
+ * tuning, solverIters); the state is the scenes' particles concatenated,
+ * scene s owning [offsets[s], offsets[s+1]).  Every scene evolves exactly as a
+ * pbf_sim with the same parameters (bit-identical), with one launch per phase
+ * over all scenes and the step captured in one CUDA graph.  Parameters are
+ * fixed at creation.  PBF_ERR_UNSUPPORTED when the scenes' particles or cells
+ * exceed 2^32 - 16 in total. */
+typedef struct pbf_ensemble pbf_ensemble;
+int pbf_ensemble_create(const pbf_sim_params* scenes, uint32_t num_scenes, pbf_ensemble** out);
+int pbf_ensemble_destroy(pbf_ensemble* ens);
+void* pbf_ensemble_stream(pbf_ensemble* ens);
+uint32_t pbf_ensemble_num_particles(pbf_ensemble* ens);
+/* offsets: num_scenes + 1 entries. */
+int pbf_ensemble_scene_offsets(pbf_ensemble* ens, uint32_t* offsets);
+int pbf_ensemble_upload_state(pbf_ensemble* ens, const float4* pos, const float4* vel);
+int pbf_ensemble_download_state(pbf_ensemble* ens, float4* pos, float4* vel);
+/* n steps, enqueued on the ensemble's stream (asynchronous). */
+int pbf_ensemble_step(pbf_ensemble* ens, int n);
+/* One step from and back to host state (pinned memory recommended). */
+int pbf_ensemble_step_host(pbf_ensemble* ens, float4* pos, float4* vel);
+int pbf_ensemble_synchronize(pbf_ensemble* ens);
+int pbf_ensemble_launches_per_step(pbf_ensemble* ens);
+
 /* Inspection: evaluates the device math the neighbour kernels use on
  * device arrays: fn 0 = powf(a, b), 1 = sqrtf(a), 2 = a / b (IEEE). */
 int pbf_debug_eval_math(int fn, const float* d_a, const float* d_b, float* d_out, uint32_t n);
