@@ -52,6 +52,12 @@ CONFIGS = {
                workload="dam_break_1M_2iter_hashed (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
     "c2_dense": dict(box=(2.0, 1.0, 2.0), lattice=(128, 64, 128), iters=2, hashed=False,
                      workload="dam_break_1M_2iter_dense (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
+    # adjoint: 32 scenes of a 64^3 lattice in a 1 m box, 60 steps, checkpoints every 10
+    # (65,536 particles per scene: a 64x32x32 lattice; a 64^3 one would hold 262,144)
+    "c5": dict(adjoint=True, scenes=32, lattice=(64, 32, 32), box=(1.0, 1.0, 1.0), iters=2, hashed=True,
+               horizon=60, every=10, res=32,
+               workload="adjoint_32x65536 (64x32x32 lattices in [0,1]^3, 2 iterations, 60 steps, checkpoints every "
+                        "10, loss on the SPH density at 32^3 grid points)"),
     # batched ensemble: 256 seeded scenes (pbfx.ensemble_scenes)
     "c4": dict(scenes=256, seed=0xE45E, iters=3, hashed=True,
                workload="ensemble_256_scenes (N_s log-uniform in [2048, 65536], boxes U[0.3,1]^3 m, gravity tilted "
@@ -406,6 +412,107 @@ def run_ours(args, cfg, world, rank, local):
     return 0
 
 
+def run_adjoint(args, cfg, world, rank, local):
+    """C5: reverse-mode gradients (pbf_forward / pbf_backward) vs the forward."""
+    import torch
+
+    import __graft_entry__ as g
+    import pbfx
+
+    if rank == 0 or world == 1:
+        g.build_library()
+    barrier(world)
+    torch.cuda.set_device(local)
+    lib = pbfx.load()
+    nx, ny, nz = cfg["lattice"]
+    n = nx * ny * nz
+    T, K, res = cfg["horizon"], cfg["every"], cfg["res"]
+    fwd_s = bwd_s = 0.0
+    losses, gnorm, cbar = [], [], []
+    for sc in range(cfg["scenes"]):
+        p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
+        pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC5000 + sc, p)
+        rng = np.random.default_rng(0xC5000 + sc)
+        vstar = np.zeros_like(pos)
+        vstar[:, :3] = rng.uniform(-0.3, 0.3, (n, 3))
+        target = torch.zeros(res ** 3, dtype=torch.float32, device="cuda")
+        with pbfx.Sim(lib, p, hashed=cfg["hashed"]) as s:
+            s.upload(pos, vstar)  # target: the density after a run from seeded velocities
+            s.step(T)
+            pbfx.check(lib.pbf_density_grid(s.h, res, C.c_void_p(target.data_ptr())))
+            v0 = np.zeros_like(pos)
+            s.upload(pos, v0)
+            s.step(1)  # graph capture outside the timing
+            s.upload(pos, v0)
+            torch.cuda.synchronize()
+            tape = C.c_void_p()
+            t0 = time.perf_counter()
+            pbfx.check(lib.pbf_forward(s.h, T, K, C.byref(tape)))
+            torch.cuda.synchronize()
+            fwd_s += time.perf_counter() - t0
+            try:
+                pbar = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+                vbar = torch.zeros_like(pbar)
+                g0 = torch.zeros_like(pbar)
+                loss, cb = C.c_double(), C.c_float()
+                pbfx.check(lib.pbf_density_grid_loss(s.h, res, C.c_void_p(target.data_ptr()), C.byref(loss),
+                                                     C.c_void_p(pbar.data_ptr())))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                pbfx.check(lib.pbf_backward(tape, C.c_void_p(pbar.data_ptr()), C.c_void_p(vbar.data_ptr()), None,
+                                            C.c_void_p(g0.data_ptr()), C.byref(cb)))
+                torch.cuda.synchronize()
+                bwd_s += time.perf_counter() - t0
+                losses.append(loss.value)
+                gnorm.append(float(torch.linalg.norm(g0[:, :3]).item()))
+                cbar.append(cb.value)
+            finally:
+                lib.pbf_tape_destroy(tape)
+    # Gradient norm against the horizon, first scene: the reference's default
+    # constants make the step chaotic (FP32 and FP64 runs separate ~10x per
+    # step), so |dL/dv0| grows geometrically with the horizon.
+    growth = {}
+    p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
+    pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC5000, p)
+    for H in (1, 2, 4, 8, 16, 32, T):
+        with pbfx.Sim(lib, p, hashed=cfg["hashed"]) as s:
+            tgt = torch.zeros(res ** 3, dtype=torch.float32, device="cuda")
+            s.upload(pos, np.zeros_like(pos))
+            tape = C.c_void_p()
+            pbfx.check(lib.pbf_forward(s.h, H, K, C.byref(tape)))
+            try:
+                pbar = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+                vbar, g0 = torch.zeros_like(pbar), torch.zeros_like(pbar)
+                loss, cb = C.c_double(), C.c_float()
+                pbfx.check(lib.pbf_density_grid_loss(s.h, res, C.c_void_p(tgt.data_ptr()), C.byref(loss),
+                                                     C.c_void_p(pbar.data_ptr())))
+                pbfx.check(lib.pbf_backward(tape, C.c_void_p(pbar.data_ptr()), C.c_void_p(vbar.data_ptr()), None,
+                                            C.c_void_p(g0.data_ptr()), C.byref(cb)))
+                growth[str(H)] = float(torch.linalg.norm(g0[:, :3]).item())
+            finally:
+                lib.pbf_tape_destroy(tape)
+    S = cfg["scenes"]
+    ratio = bwd_s / fwd_s
+    line = {
+        "metric": "adjoint/fwd time", "value": ratio, "unit": "backward time / forward time", "n_gpus": world,
+        "steps": T, "warmup": 1, "ms_per_step": 1e3 * (fwd_s + bwd_s) / (S * T), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattices)",
+        "config": {"workload": cfg["workload"], "scenes": S, "particles_per_scene": n, "solver_iters": cfg["iters"],
+                   "checkpoint_every": K, "grid_points": res ** 3, "parallelism": "single"},
+        "forward_ms_per_step": 1e3 * fwd_s / (S * T), "backward_ms_per_step": 1e3 * bwd_s / (S * T),
+        "backward_includes": "the replay of each checkpoint segment (one recorded forward step per step) and the "
+                             "adjoint kernels",
+        "loss_mean": float(np.mean(losses)), "grad_v0_norm_mean": float(np.mean(gnorm)),
+        "grad_xsph_c_mean": float(np.mean(cbar)),
+        "grad_v0_norm_by_horizon": growth,
+        "e2e": {"value": ratio, "unit": "backward time / forward time", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0, "note": "host wall clock around pbf_forward / pbf_backward"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ensemble(args, cfg, world, rank, local):
     """C4: the batched ensemble vs the same scenes stepped one by one."""
     import torch
@@ -561,11 +668,16 @@ def main(argv=None):
     world, rank, local = dist_setup()
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
+        if cfg.get("adjoint"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}))
+            return 0
         if "scenes" in cfg:
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched ensemble; "
                               "bench.py --config c4 reports its looped kernels as reference_gpu_looped"}))
             return 0
         return run_reference(args, cfg, world, rank)
+    if cfg.get("adjoint"):
+        return run_adjoint(args, cfg, world, rank, local)
     if "scenes" in cfg:
         return run_ensemble(args, cfg, world, rank, local)
     return run_ours(args, cfg, world, rank, local)

@@ -1,0 +1,784 @@
+// adjoint.cu - reverse-mode gradients of the PBF step.
+//
+// No counterpart in the reference.  pbf_forward runs a handle's scene for n
+// steps and keeps (pos, vel) checkpoints every k steps; pbf_backward takes
+// dL/d(final pos, final vel) and returns dL/d(initial pos, initial vel) and
+// dL/d(xsph_c).  Each checkpoint segment is replayed once, recording every
+// step's intermediates (the fused step's own launchers writing into record
+// buffers: predictions of every solver iteration, lambdas, the solved
+// prediction, the velocity before XSPH, the sorted keys, permutation and
+// lower-bound table), then the steps are differentiated in reverse.
+//
+// The derivative is that of the step as written (sim/integrate.cu,
+// sim/pbf_lambda.cu, sim/pbf_delta_apply.cu, sim/xsph.cu, sim/boundary.cu),
+// with neighbour sets held fixed within a step: a pair contributes where the
+// forward found it within h (lambda: among the first maxNeighbors in walk
+// order).  Clamps contribute the derivative of the branch taken: a clamped
+// position axis, a clamped lambda, a lambda zeroed for too few neighbours and
+// an s_corr held at its floor pass no gradient; the displacement clamp passes
+// the Jacobian of d * maxDisp / |d|.  Every particle gathers its own terms;
+// terms that belong to a neighbour are added to it with float atomics, so
+// gradients agree run to run only to rounding.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/pbf/pbf.h"
+#include "../../include/pbf/simulator.h"
+#include "fused.cuh"
+#include "handle.h"
+#include "grid.cuh"
+#include "pbf_common.cuh"
+#include "sort.cuh"
+
+namespace pbf {
+namespace {
+
+constexpr int kBS = 256;
+constexpr int kAdjBS = 128;
+
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ void atomic_add3(float4* p, float3 v) {
+    atomicAdd(&p->x, v.x);
+    atomicAdd(&p->y, v.y);
+    atomicAdd(&p->z, v.z);
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Pair geometry of (i, j) as the forward computes it: u = x_i - x_j, r2, and
+// the spiky gradient a = coeff(r) u with its Jacobian applied to a vector.
+struct Pair {
+    float3 u;
+    float r2, r, coeff, dcoeff;  // dcoeff = d coeff / d r
+};
+
+__device__ __forceinline__ Pair pair_of(float4 xi, float4 xj, const sim::DeviceParams& dp) {
+    Pair q;
+    float rx, ry, rz;
+    q.r2 = dist2(xi, xj, rx, ry, rz);
+    q.u = make_float3(rx, ry, rz);
+    q.r = sqrt_(q.r2);
+    const float h = dp.kernel.h, s = dp.kernel.spiky, eps = dp.pbf.grad_r_eps;
+    const float t = h - q.r;
+    const float rs = fmaxf(q.r, eps);
+    q.coeff = div_(mul_(mul_(-3.0f, s), mul_(t, t)), rs);
+    // coeff(r) = -3 s (h - r)^2 / max(r, eps)
+    q.dcoeff = (q.r > eps) ? 3.0f * s * t * (h + q.r) / (q.r * q.r) : 6.0f * s * t / eps;
+    return q;
+}
+
+// J^T g for J = d a / d u = coeff I + (coeff'/r) u u^T.
+__device__ __forceinline__ float3 jt(const Pair& q, float3 g) {
+    const float k = (q.r > 0.f) ? q.dcoeff / q.r * dot3(q.u, g) : 0.f;
+    return make_float3(q.coeff * g.x + k * q.u.x, q.coeff * g.y + k * q.u.y, q.coeff * g.z + k * q.u.z);
+}
+
+// Candidates of slot s: stencil rows of its start-of-step cell.
+template <class Visit>
+__device__ __forceinline__ void for_candidates(uint32_t s, const uint32_t* __restrict__ key_s,
+                                               const uint32_t* __restrict__ lb, const sim::DeviceParams& dp,
+                                               Visit&& visit) {
+    int cx, cy, cz;
+    decode_key(key_s[s], dp.grid.dim, cx, cy, cz);
+    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, visit);
+}
+
+// ---------------------------------------------------------------- XSPH
+// v''_i = v_i + c g (m / rho0) sum_j (v_j - v_i) W_ij at the solved positions.
+__global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ xf, const float4* __restrict__ vf,
+                                                     const uint32_t* __restrict__ key_s,
+                                                     const uint32_t* __restrict__ lb,
+                                                     const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                     const float4* __restrict__ vbar_out, float4* __restrict__ vfbar,
+                                                     float4* __restrict__ xfbar, float* __restrict__ cbar) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    float cpart = 0.f;
+    if (s < N) {
+        const sim::DeviceParams& dp = *dpp;
+        const float4 xi = xf[s], vi = vf[s];
+        const float3 g = f3(vbar_out[s]);
+        // forward: count and sum, for the gate and dL/dc
+        int count = 0;
+        float wsum = 0.f;
+        float3 sum = make_float3(0.f, 0.f, 0.f);
+        for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+            if (k == s) return true;
+            float rx, ry, rz;
+            const float r2 = dist2(xi, xf[k], rx, ry, rz);
+            if (r2 > dp.kernel.h2) return true;
+            const float hr2 = sub_(dp.kernel.h2, r2);
+            const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
+            const float4 vj = vf[k];
+            sum.x += (vj.x - vi.x) * w;
+            sum.y += (vj.y - vi.y) * w;
+            sum.z += (vj.z - vi.z) * w;
+            wsum += w;
+            ++count;
+            return true;
+        });
+        float gate = 1.0f;
+        if (dp.pbf.xsph_gate_enable) {
+            const int nMin = max(0, dp.pbf.xsph_n_min);
+            const int nMax = max(nMin + 1, dp.pbf.xsph_n_max);
+            gate = fminf(1.f, fmaxf(0.f, (float(count) - float(nMin)) / float(nMax - nMin)));
+        }
+        const float mor = (dp.restDensity > 0.f) ? dp.particleMass / dp.restDensity : 0.f;
+        const float ceff = dp.xsph_c * gate * mor;
+        cpart = gate * mor * dot3(sum, g);
+        atomic_add3(vfbar + s, make_float3(g.x - ceff * wsum * g.x, g.y - ceff * wsum * g.y, g.z - ceff * wsum * g.z));
+        float3 own = make_float3(0.f, 0.f, 0.f);
+        for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+            if (k == s) return true;
+            float rx, ry, rz;
+            const float r2 = dist2(xi, xf[k], rx, ry, rz);
+            if (r2 > dp.kernel.h2) return true;
+            const float hr2 = sub_(dp.kernel.h2, r2);
+            const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
+            const float4 vj = vf[k];
+            atomic_add3(vfbar + k, make_float3(ceff * w * g.x, ceff * w * g.y, ceff * w * g.z));
+            const float wbar = ceff * ((vj.x - vi.x) * g.x + (vj.y - vi.y) * g.y + (vj.z - vi.z) * g.z);
+            const float r2bar = wbar * (-3.0f * dp.kernel.poly6 * hr2 * hr2);
+            const float3 ub = make_float3(2.f * rx * r2bar, 2.f * ry * r2bar, 2.f * rz * r2bar);
+            own.x += ub.x;
+            own.y += ub.y;
+            own.z += ub.z;
+            atomic_add3(xfbar + k, make_float3(-ub.x, -ub.y, -ub.z));
+            return true;
+        });
+        atomic_add3(xfbar + s, own);
+    }
+    // dL/dc: block sum, one atomic per block
+    __shared__ float red[kAdjBS];
+    red[threadIdx.x] = cpart;
+    __syncthreads();
+    for (int w = kAdjBS / 2; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && cbar) atomicAdd(cbar, red[0]);
+}
+
+// v_f = (x_f - p) / dt; x_f = clamp(x_iters).  Writes dL/dx_iters and
+// dL/dp (sorted).
+__global__ void __launch_bounds__(kBS) k_adj_velocity(const float4* __restrict__ xf,
+                                                      const float4* __restrict__ vfbar,
+                                                      const float4* __restrict__ xfbar,
+                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                      float4* __restrict__ xbar, float4* __restrict__ pbar_s,
+                                                      int iters) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const float inv_dt = 1.0f / dp.dt;
+    const float4 vb = vfbar[s], xb = xfbar[s], x = xf[s];
+    float3 g = make_float3(xb.x + vb.x * inv_dt, xb.y + vb.y * inv_dt, xb.z + vb.z * inv_dt);
+    pbar_s[s] = make_float4(-vb.x * inv_dt, -vb.y * inv_dt, -vb.z * inv_dt, 0.f);
+    // the post-solve clamp (only when iterations ran; otherwise x_f is the
+    // prediction, whose own clamp the predict adjoint applies)
+    if (iters > 0) {
+        const sim::GridBounds& gb = dp.grid;
+        if (x.x <= gb.mins.x || x.x >= gb.maxs.x) g.x = 0.f;
+        if (x.y <= gb.mins.y || x.y >= gb.maxs.y) g.y = 0.f;
+        if (x.z <= gb.mins.z || x.z >= gb.maxs.z) g.z = 0.f;
+    }
+    xbar[s] = make_float4(g.x, g.y, g.z, 0.f);
+}
+
+// ----------------------------------------------------------------- delta
+// x^{k+1}_i = x^k_i + clampDisp(relax / rho0 * sum_j (l_i + l_j + scorr_ij) a_ij)
+__global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__ x, const float* __restrict__ lam,
+                                                      const uint32_t* __restrict__ key_s,
+                                                      const uint32_t* __restrict__ lb,
+                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                      const float4* __restrict__ xbar_in,
+                                                      float4* __restrict__ xbar_out, float* __restrict__ lambar) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const sim::PbfTuning& pbf = dp.pbf;
+    const float4 xi = x[s];
+    const float li = lam[s];
+    const float w_q = scorr_wq(dp);
+    const float3 gin = f3(xbar_in[s]);
+    // forward displacement, for the clamp
+    float3 D = make_float3(0.f, 0.f, 0.f);
+    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+        if (k == s) return true;
+        float rx, ry, rz;
+        const float r2 = dist2(xi, x[k], rx, ry, rz);
+        if (r2 > dp.kernel.h2) return true;
+        delta_accumulate(D, rx, ry, rz, r2, li, lam[k], w_q, dp);
+        return true;
+    });
+    const float invRest = (dp.restDensity > 0.f) ? 1.0f / dp.restDensity : 0.f;
+    const float omega = pbf.enable_relax ? pbf.relax_omega : 1.0f;
+    const float3 d = make_float3(D.x * invRest * omega, D.y * invRest * omega, D.z * invRest * omega);
+    float3 db = gin;
+    if (pbf.enable_disp_clamp) {
+        const float md = pbf.disp_clamp_max_h * dp.kernel.h;
+        const float L2 = dot3(d, d);
+        if (L2 > md * md) {
+            const float L = sqrtf(L2);
+            const float sc = md / (L + 1e-20f);
+            const float proj = dot3(d, gin) / L2;
+            db = make_float3(sc * (gin.x - d.x * proj), sc * (gin.y - d.y * proj), sc * (gin.z - d.z * proj));
+        }
+    }
+    const float3 Db = make_float3(db.x * invRest * omega, db.y * invRest * omega, db.z * invRest * omega);
+    float lown = 0.f;
+    float3 own = gin;  // identity path x^k -> x^{k+1}
+    const float kcorr = pbf.scorr_k, ncorr = pbf.scorr_n;
+    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+        if (k == s) return true;
+        const Pair q = pair_of(xi, x[k], dp);
+        if (q.r2 > dp.kernel.h2) return true;
+        const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
+        float scorr = 0.f, dscorr = 0.f;  // d scorr / d r2
+        if (pbf.scorr_enable) {
+            const float hr2 = dp.kernel.h2 - q.r2;
+            const float w = dp.kernel.poly6 * hr2 * hr2 * hr2;
+            const float ratio = (w_q > 0.f) ? w / w_q : 0.f;
+            scorr = -kcorr * powf(ratio, ncorr);
+            const bool floored = pbf.scorr_min < 0.f && scorr < pbf.scorr_min;
+            if (floored) scorr = pbf.scorr_min;
+            if (!floored && w_q > 0.f && ratio > 0.f)
+                dscorr = -kcorr * ncorr * powf(ratio, ncorr - 1.0f) * (-3.0f * dp.kernel.poly6 * hr2 * hr2) / w_q;
+        }
+        const float lij = li + lam[k] + scorr;
+        const float lbar = dot3(Db, a);
+        lown += lbar;
+        atomicAdd(lambar + k, lbar);
+        float3 ub = jt(q, make_float3(lij * Db.x, lij * Db.y, lij * Db.z));
+        const float r2bar = lbar * dscorr;
+        ub.x += 2.f * q.u.x * r2bar;
+        ub.y += 2.f * q.u.y * r2bar;
+        ub.z += 2.f * q.u.z * r2bar;
+        own.x += ub.x;
+        own.y += ub.y;
+        own.z += ub.z;
+        atomic_add3(xbar_out + k, make_float3(-ub.x, -ub.y, -ub.z));
+        return true;
+    });
+    atomicAdd(lambar + s, lown);
+    atomic_add3(xbar_out + s, own);
+}
+
+// ---------------------------------------------------------------- lambda
+// lambda_i = -(rho_i / rho0 - 1) / (scale^2 (sum_j |a_ij|^2 + |sum_j a_ij|^2) + eps)
+__global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict__ x,
+                                                       const uint32_t* __restrict__ key_s,
+                                                       const uint32_t* __restrict__ lb,
+                                                       const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                       const float* __restrict__ lambar,
+                                                       float4* __restrict__ xbar_out) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const sim::PbfTuning& pbf = dp.pbf;
+    const float lb_i = lambar[s];
+    if (lb_i == 0.f) return;
+    const float4 xi = x[s];
+    const int cap = dp.maxNeighbors > 0 ? dp.maxNeighbors : 0x7FFFFFFF;
+    LambdaAcc acc;
+    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+        if (acc.contrib >= cap) return false;
+        if (k == s) return true;
+        float rx, ry, rz;
+        const float r2 = dist2(xi, x[k], rx, ry, rz);
+        if (r2 > dp.kernel.h2) return true;
+        lambda_accumulate(acc, rx, ry, rz, r2, dp);
+        return true;
+    });
+    // the forward's branches (lambda_finalize)
+    const float rho0 = dp.restDensity;
+    const float scale = (rho0 > 0.f) ? dp.particleMass / rho0 : 0.f;
+    const float G2 = acc.gx * acc.gx + acc.gy * acc.gy + acc.gz * acc.gz;
+    const float sum = acc.sumGrad2 + G2;
+    float denom0 = scale * scale * sum + pbf.lambda_denom_eps;
+    if (pbf.compliance > 0.f && dp.dt > 0.f) denom0 += pbf.compliance / (dp.dt * dp.dt);
+    const float denom = fmaxf(denom0, pbf.lambda_denom_eps);
+    if (acc.contrib < 2 || sum < 1e-12f || !(rho0 > 0.f)) return;
+    const float C = acc.density / rho0 - 1.f;
+    const float lam = -C / denom;
+    if (!isfinite(lam)) return;
+    if (pbf.enable_lambda_clamp && fabsf(lam) > pbf.lambda_max_abs) return;
+    const float Cb = -lb_i / denom;
+    const float denb = (denom0 >= pbf.lambda_denom_eps) ? -lb_i * lam / denom : 0.f;
+    const float sb = denb * scale * scale;
+    const float rhob = Cb / rho0;
+    const float3 G = make_float3(acc.gx, acc.gy, acc.gz);
+    float3 own = make_float3(0.f, 0.f, 0.f);
+    int seen = 0;
+    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+        if (seen >= cap) return false;
+        if (k == s) return true;
+        const Pair q = pair_of(xi, x[k], dp);
+        if (q.r2 > dp.kernel.h2) return true;
+        ++seen;
+        const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
+        const float hr2 = dp.kernel.h2 - q.r2;
+        const float r2bar = -3.0f * rhob * dp.particleMass * dp.kernel.poly6 * hr2 * hr2;
+        float3 ub = jt(q, make_float3(2.f * sb * (a.x + G.x), 2.f * sb * (a.y + G.y), 2.f * sb * (a.z + G.z)));
+        ub.x += 2.f * q.u.x * r2bar;
+        ub.y += 2.f * q.u.y * r2bar;
+        ub.z += 2.f * q.u.z * r2bar;
+        own.x += ub.x;
+        own.y += ub.y;
+        own.z += ub.z;
+        atomic_add3(xbar_out + k, make_float3(-ub.x, -ub.y, -ub.z));
+        return true;
+    });
+    atomic_add3(xbar_out + s, own);
+}
+
+// ---------------------------------------------------------------- predict
+// x^0 = clamp(p + (v + g dt) dt); scatter dL/dp and dL/dv to particle ids.
+__global__ void __launch_bounds__(kBS) k_adj_predict(const float4* __restrict__ x0,
+                                                     const float4* __restrict__ xbar0,
+                                                     const float4* __restrict__ pbar_s,
+                                                     const uint32_t* __restrict__ perm,
+                                                     const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                     float4* __restrict__ pbar, float4* __restrict__ vbar) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const sim::GridBounds& gb = dp.grid;
+    const float4 x = x0[s];
+    float3 g = f3(xbar0[s]);
+    if (x.x <= gb.mins.x || x.x >= gb.maxs.x) g.x = 0.f;
+    if (x.y <= gb.mins.y || x.y >= gb.maxs.y) g.y = 0.f;
+    if (x.z <= gb.mins.z || x.z >= gb.maxs.z) g.z = 0.f;
+    const float4 pb = pbar_s[s];
+    const uint32_t i = perm[s];
+    pbar[i] = make_float4(pb.x + g.x, pb.y + g.y, pb.z + g.z, 0.f);
+    vbar[i] = make_float4(dp.dt * g.x, dp.dt * g.y, dp.dt * g.z, 0.f);
+}
+
+// dL/d(outputs) of a step in sorted order: x_f[s] is p_{n+1}[perm[s]].
+__global__ void __launch_bounds__(kBS) k_adj_gather_out(const uint32_t* __restrict__ perm,
+                                                        const float4* __restrict__ pbar,
+                                                        const float4* __restrict__ vbar, uint32_t N,
+                                                        float4* __restrict__ xfbar, float4* __restrict__ vxbar) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const uint32_t i = perm[s];
+    xfbar[s] = pbar[i];
+    vxbar[s] = vbar[i];
+}
+
+// --------------------------------------------------------- grid density loss
+// rho(g) = sum_i m W(|g - p_i|) on res^3 cell centres of the box.
+struct GridDesc {
+    float3 lo, step;
+    int res;
+};
+
+__device__ __forceinline__ void grid_range(float c, float lo, float step, float h, int res, int& a, int& b) {
+    a = max(0, int(ceilf((c - h - lo) / step - 0.5f)));
+    b = min(res - 1, int(floorf((c + h - lo) / step - 0.5f)));
+}
+
+__global__ void __launch_bounds__(kBS) k_grid_density(const float4* __restrict__ pos,
+                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                      GridDesc gd, float* __restrict__ rho) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const float h = dp.kernel.h, h2 = dp.kernel.h2;
+    const float4 p = pos[i];
+    int x0, x1, y0, y1, z0, z1;
+    grid_range(p.x, gd.lo.x, gd.step.x, h, gd.res, x0, x1);
+    grid_range(p.y, gd.lo.y, gd.step.y, h, gd.res, y0, y1);
+    grid_range(p.z, gd.lo.z, gd.step.z, h, gd.res, z0, z1);
+    for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                const float gx = gd.lo.x + (x + 0.5f) * gd.step.x, gy = gd.lo.y + (y + 0.5f) * gd.step.y,
+                            gz = gd.lo.z + (z + 0.5f) * gd.step.z;
+                const float dx = gx - p.x, dy = gy - p.y, dz = gz - p.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 >= h2) continue;
+                const float hr2 = h2 - r2;
+                atomicAdd(rho + (size_t(z) * gd.res + y) * gd.res + x, dp.particleMass * dp.kernel.poly6 * hr2 * hr2 * hr2);
+            }
+}
+
+// Residuals r = rho - target and the loss sum (one partial per block).
+__global__ void __launch_bounds__(kBS) k_grid_residual(float* __restrict__ rho, const float* __restrict__ target,
+                                                       uint32_t G, double* __restrict__ partial) {
+    __shared__ double red[kBS];
+    double acc = 0.0;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x) {
+        const float r = rho[g] - target[g];
+        rho[g] = r;
+        acc += double(r) * double(r);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kBS / 2; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// dL/dp_i = 2/G sum_g r_g m dW(g - p_i)/dp_i.
+__global__ void __launch_bounds__(kBS) k_grid_loss_grad(const float4* __restrict__ pos,
+                                                        const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                        GridDesc gd, const float* __restrict__ resid,
+                                                        float scale, float4* __restrict__ pbar) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const float h = dp.kernel.h, h2 = dp.kernel.h2;
+    const float4 p = pos[i];
+    int x0, x1, y0, y1, z0, z1;
+    grid_range(p.x, gd.lo.x, gd.step.x, h, gd.res, x0, x1);
+    grid_range(p.y, gd.lo.y, gd.step.y, h, gd.res, y0, y1);
+    grid_range(p.z, gd.lo.z, gd.step.z, h, gd.res, z0, z1);
+    float3 g = make_float3(0.f, 0.f, 0.f);
+    for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                const float gx = gd.lo.x + (x + 0.5f) * gd.step.x, gy = gd.lo.y + (y + 0.5f) * gd.step.y,
+                            gz = gd.lo.z + (z + 0.5f) * gd.step.z;
+                const float dx = p.x - gx, dy = p.y - gy, dz = p.z - gz;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 >= h2) continue;
+                const float hr2 = h2 - r2;
+                // dW/dp = poly6 * 3 hr2^2 * (-2 (p - g))
+                const float c = scale * resid[(size_t(z) * gd.res + y) * gd.res + x] * dp.particleMass *
+                                dp.kernel.poly6 * (-6.0f) * hr2 * hr2;
+                g.x += c * dx;
+                g.y += c * dy;
+                g.z += c * dz;
+            }
+    pbar[i] = make_float4(g.x, g.y, g.z, 0.f);
+}
+
+template <class T>
+bool dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count) == cudaSuccess;
+}
+
+int status_of(cudaError_t e) {
+    if (e == cudaSuccess) return PBF_OK;
+    if (e == cudaErrorMemoryAllocation) return PBF_ERR_OOM;
+    return PBF_ERR_CUDA;
+}
+
+GridDesc grid_desc(const sim::GridBounds& g, int res) {
+    GridDesc d;
+    d.res = res;
+    d.lo = g.mins;
+    d.step = make_float3((g.maxs.x - g.mins.x) / res, (g.maxs.y - g.mins.y) / res, (g.maxs.z - g.mins.z) / res);
+    return d;
+}
+
+// One step's recorded intermediates (sorted order).
+struct StepRecord {
+    std::vector<float4*> x;  // x[0..iters]: predictions of each iteration; x[iters] = solved (clamped)
+    std::vector<float*> lam;  // lambda of each iteration
+    float4* vf = nullptr;     // velocity before XSPH
+    float4* ps = nullptr;     // step-start positions
+    uint32_t* key_s = nullptr;
+    uint32_t* perm = nullptr;
+    uint32_t* lb = nullptr;
+};
+
+}  // namespace
+}  // namespace pbf
+
+struct pbf_tape {
+    sim::SimParams p{};
+    uint32_t N = 0, numCells = 0;
+    int steps = 0, every = 1, iters = 0, keyBits = 1;
+    bool xsph = false;
+    cudaStream_t stream = nullptr;
+    // replay engine (the fused step's buffers)
+    float4 *pos = nullptr, *vel = nullptr;
+    uint32_t* keys = nullptr;
+    sim::DeviceParams* dp = nullptr;
+    uint32_t* err = nullptr;
+    void* sortTemp = nullptr;
+    size_t sortBytes = 0;
+    // checkpoints (device): state at steps 0, every, 2 every, ...
+    std::vector<float4*> ckPos, ckVel;
+    std::vector<pbf::StepRecord> rec;  // one segment
+    // adjoint scratch
+    float4 *pbar = nullptr, *vbar = nullptr, *xfbar = nullptr, *vxbar = nullptr, *vfbar = nullptr, *xbA = nullptr,
+           *xbB = nullptr, *pbar_s = nullptr;
+    float *lambar = nullptr, *cbar = nullptr;
+    std::vector<void*> owned;
+
+    template <class T>
+    bool alloc(T** ptr, size_t count) {
+        if (!pbf::dalloc(ptr, count)) return false;
+        owned.push_back(*ptr);
+        return true;
+    }
+    ~pbf_tape() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (void* q : owned) cudaFree(q);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    pbf::FusedShape shape() const {
+        pbf::FusedShape sh{};
+        sh.N = N;
+        sh.numCells = numCells;
+        sh.key_bits = keyBits;
+        sh.iters = iters;
+        sh.hashed = false;
+        sh.xsph = xsph;
+        sh.list_span = 0;
+        return sh;
+    }
+
+    // Steps the replay engine once, recording into r.
+    cudaError_t record_step(const pbf::StepRecord& r) {
+        using namespace pbf;
+        const FusedShape sh = shape();
+        FusedBufs b{};
+        b.pos = pos;
+        b.vel = vel;
+        b.keys = keys;
+        b.key_s = r.key_s;
+        b.perm = r.perm;
+        b.pred_a = r.x[0];
+        b.pred_b = r.x[0];
+        b.pos_s = r.ps;
+        b.vel_s = r.vf;
+        b.lam_s = r.lam.empty() ? nullptr : r.lam[0];
+        b.lb = r.lb;
+        b.sort_temp = sortTemp;
+        b.sort_bytes = sortBytes;
+        b.dp = dp;
+        b.err = err;
+        cudaError_t e;
+        if ((e = fused_predict_keys(b, sh, stream)) != cudaSuccess) return e;
+        if ((e = fused_sort(b, sh, stream)) != cudaSuccess) return e;
+        if ((e = fused_gather_and_tables(b, sh, stream)) != cudaSuccess) return e;
+        if (iters <= 0) {
+            if ((e = fused_solve(b, sh, stream)) != cudaSuccess) return e;  // boundary + velocity on x[0]
+        }
+        for (int it = 0; it < iters; ++it) {
+            FusedBufs bi = b;
+            float4* cur = r.x[it];
+            float4* nxt = r.x[it + 1];
+            bi.pred_a = (it % 2 == 0) ? cur : nxt;
+            bi.pred_b = (it % 2 == 0) ? nxt : cur;
+            bi.lam_s = r.lam[it];
+            if ((e = fused_solve_phase(bi, sh, it, 0, stream)) != cudaSuccess) return e;
+            if ((e = fused_solve_phase(bi, sh, it, 1, stream)) != cudaSuccess) return e;
+        }
+        FusedBufs bc = b;
+        bc.pred_a = bc.pred_b = r.x[std::max(iters, 0)];
+        return fused_commit(bc, sh, stream);
+    }
+
+    // dL/d(outputs of the recorded step) in pbar/vbar (ids) -> dL/d(inputs).
+    cudaError_t adjoint_step(const pbf::StepRecord& r) {
+        using namespace pbf;
+        const unsigned g = blocks_for(N, kBS), ga = blocks_for(N, kAdjBS);
+        const size_t b4 = sizeof(float4) * N;
+        k_adj_gather_out<<<g, kBS, 0, stream>>>(r.perm, pbar, vbar, N, xfbar, vxbar);
+        const float4* xf = r.x[std::max(iters, 0)];
+        if (xsph) {
+            cudaMemsetAsync(vfbar, 0, b4, stream);
+            k_adj_xsph<<<ga, kAdjBS, 0, stream>>>(xf, r.vf, r.key_s, r.lb, dp, N, vxbar, vfbar, xfbar, cbar);
+        } else {
+            cudaMemcpyAsync(vfbar, vxbar, b4, cudaMemcpyDeviceToDevice, stream);
+        }
+        k_adj_velocity<<<g, kBS, 0, stream>>>(xf, vfbar, xfbar, dp, N, xbA, pbar_s, iters);
+        float4* xin = xbA;
+        float4* xout = xbB;
+        for (int it = iters - 1; it >= 0; --it) {
+            cudaMemsetAsync(xout, 0, b4, stream);
+            cudaMemsetAsync(lambar, 0, sizeof(float) * N, stream);
+            k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], r.key_s, r.lb, dp, N, xin, xout, lambar);
+            k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.key_s, r.lb, dp, N, lambar, xout);
+            std::swap(xin, xout);
+        }
+        k_adj_predict<<<g, kBS, 0, stream>>>(r.x[0], xin, pbar_s, r.perm, dp, N, pbar, vbar);
+        return cudaGetLastError();
+    }
+};
+
+namespace {
+
+int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool xsph, pbf_tape** out) {
+    using namespace pbf;
+    pbf_tape* t = new (std::nothrow) pbf_tape;
+    if (!t) return PBF_ERR_OOM;
+    t->p = sp;
+    t->N = N;
+    t->steps = steps;
+    t->every = every;
+    t->iters = sp.solverIters;
+    t->xsph = xsph;
+    const int3 d = sp.grid.dim;
+    t->numCells = uint32_t(d.x) * uint32_t(d.y) * uint32_t(d.z);
+    t->keyBits = bits_for(t->numCells - 1u);
+    t->sortBytes = sort_temp_bytes(N, t->keyBits);
+    const int segs = (steps + every - 1) / every;
+    bool ok = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) == cudaSuccess && t->alloc(&t->pos, N) &&
+              t->alloc(&t->vel, N) && t->alloc(&t->keys, N) && t->alloc(&t->dp, 1) && t->alloc(&t->err, 1) &&
+              t->alloc(reinterpret_cast<unsigned char**>(&t->sortTemp), t->sortBytes) && t->alloc(&t->pbar, N) &&
+              t->alloc(&t->vbar, N) && t->alloc(&t->xfbar, N) && t->alloc(&t->vxbar, N) && t->alloc(&t->vfbar, N) &&
+              t->alloc(&t->xbA, N) && t->alloc(&t->xbB, N) && t->alloc(&t->pbar_s, N) && t->alloc(&t->lambar, N) &&
+              t->alloc(&t->cbar, 1);
+    for (int c = 0; ok && c < segs; ++c) {
+        float4 *cp = nullptr, *cv = nullptr;
+        ok = t->alloc(&cp, N) && t->alloc(&cv, N);
+        t->ckPos.push_back(cp);
+        t->ckVel.push_back(cv);
+    }
+    t->rec.resize(size_t(std::min(every, steps)));
+    for (auto& r : t->rec) {
+        if (!ok) break;
+        r.x.assign(size_t(std::max(t->iters, 0) + 1), nullptr);
+        r.lam.assign(size_t(std::max(t->iters, 0)), nullptr);
+        for (auto& x : r.x) ok = ok && t->alloc(&x, N);
+        for (auto& l : r.lam) ok = ok && t->alloc(&l, N);
+        ok = ok && t->alloc(&r.vf, N) && t->alloc(&r.ps, N) && t->alloc(&r.key_s, N) && t->alloc(&r.perm, N) &&
+             t->alloc(&r.lb, size_t(t->numCells) + 1);
+    }
+    if (ok) {
+        const sim::DeviceParams dp = sim::MakeDeviceParams(sp);
+        ok = cudaMemcpy(t->dp, &dp, sizeof(dp), cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemset(t->err, 0, sizeof(uint32_t)) == cudaSuccess;
+    }
+    if (!ok) {
+        const cudaError_t e = cudaGetLastError();
+        delete t;
+        return e == cudaErrorMemoryAllocation ? PBF_ERR_OOM : PBF_ERR_CUDA;
+    }
+    *out = t;
+    return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbf_forward(pbf_sim* h, int steps, int checkpoint_every, pbf_tape** out) {
+    if (!out) return PBF_ERR_INVALID;
+    *out = nullptr;
+    if (!h || steps <= 0 || checkpoint_every <= 0) return PBF_ERR_INVALID;
+    sim::Simulator& S = h->sim;
+    const sim::SimParams& sp = S.params();
+    const uint32_t N = S.activeParticleCount();
+    if (sp.pbf.xpbd_enable) return PBF_ERR_UNSUPPORTED;
+    pbf_tape* t = nullptr;
+    int st = make_tape(sp, N, steps, checkpoint_every, S.buffers().xsphEnabled && sp.xsph_c > 0.f, &t);
+    if (st != PBF_OK) return st;
+    const size_t b4 = sizeof(float4) * N;
+    cudaStream_t s = S.cudaStream();
+    for (int n = 0; n < steps; ++n) {
+        if (n % checkpoint_every == 0) {
+            const int c = n / checkpoint_every;
+            cudaMemcpyAsync(t->ckPos[c], S.devicePositions(), b4, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(t->ckVel[c], S.deviceVel(), b4, cudaMemcpyDeviceToDevice, s);
+        }
+        if (!S.step(sp)) {
+            delete t;
+            return PBF_ERR_CUDA;
+        }
+    }
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        delete t;
+        return pbf::status_of(e);
+    }
+    *out = t;
+    return PBF_OK;
+}
+
+int pbf_backward(pbf_tape* t, const float4* d_pos_bar, const float4* d_vel_bar, float4* d_pos0_bar,
+                 float4* d_vel0_bar, float* xsph_c_bar) {
+    if (!t || !d_pos_bar || !d_vel_bar) return PBF_ERR_INVALID;
+    const size_t b4 = sizeof(float4) * t->N;
+    cudaStream_t s = t->stream;
+    cudaMemcpyAsync(t->pbar, d_pos_bar, b4, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(t->vbar, d_vel_bar, b4, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(t->cbar, 0, sizeof(float), s);
+    const int segs = int(t->ckPos.size());
+    for (int c = segs - 1; c >= 0; --c) {
+        const int start = c * t->every;
+        const int len = std::min(t->every, t->steps - start);
+        cudaMemcpyAsync(t->pos, t->ckPos[c], b4, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(t->vel, t->ckVel[c], b4, cudaMemcpyDeviceToDevice, s);
+        for (int n = 0; n < len; ++n)
+            if (t->record_step(t->rec[n]) != cudaSuccess) return PBF_ERR_CUDA;
+        for (int n = len - 1; n >= 0; --n)
+            if (t->adjoint_step(t->rec[n]) != cudaSuccess) return PBF_ERR_CUDA;
+    }
+    if (d_pos0_bar) cudaMemcpyAsync(d_pos0_bar, t->pbar, b4, cudaMemcpyDeviceToDevice, s);
+    if (d_vel0_bar) cudaMemcpyAsync(d_vel0_bar, t->vbar, b4, cudaMemcpyDeviceToDevice, s);
+    float cb = 0.f;
+    cudaMemcpyAsync(&cb, t->cbar, sizeof(float), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return pbf::status_of(e);
+    uint32_t err = 0;
+    cudaMemcpy(&err, t->err, sizeof(err), cudaMemcpyDeviceToHost);
+    if (err) return (err & pbf::kErrLookbackTimeoutBit) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
+    if (xsph_c_bar) *xsph_c_bar = cb;
+    return PBF_OK;
+}
+
+int pbf_tape_destroy(pbf_tape* t) {
+    delete t;
+    return PBF_OK;
+}
+
+int pbf_density_grid(pbf_sim* h, int res, float* d_grid) {
+    if (!h || res <= 0 || res > 1024 || !d_grid) return PBF_ERR_INVALID;
+    sim::Simulator& S = h->sim;
+    const uint32_t N = S.activeParticleCount();
+    cudaStream_t s = S.cudaStream();
+    const size_t G = size_t(res) * res * res;
+    cudaMemsetAsync(d_grid, 0, sizeof(float) * G, s);
+    if (N > 0)
+        pbf::k_grid_density<<<pbf::blocks_for(N, pbf::kBS), pbf::kBS, 0, s>>>(
+            S.devicePositions(), S.buffers().d_params, N, pbf::grid_desc(S.params().grid, res), d_grid);
+    return pbf::status_of(cudaStreamSynchronize(s));
+}
+
+int pbf_density_grid_loss(pbf_sim* h, int res, const float* d_target, double* loss, float4* d_pos_bar) {
+    if (!h || res <= 0 || res > 1024 || !d_target) return PBF_ERR_INVALID;
+    sim::Simulator& S = h->sim;
+    const uint32_t N = S.activeParticleCount();
+    cudaStream_t s = S.cudaStream();
+    const uint32_t G = uint32_t(res) * res * res;
+    float* rho = nullptr;
+    double* partial = nullptr;
+    const unsigned nb = std::min<unsigned>(1024u, pbf::blocks_for(G, pbf::kBS));
+    if (cudaMallocAsync(&rho, sizeof(float) * G, s) != cudaSuccess ||
+        cudaMallocAsync(&partial, sizeof(double) * nb, s) != cudaSuccess)
+        return PBF_ERR_OOM;
+    const pbf::GridDesc gd = pbf::grid_desc(S.params().grid, res);
+    cudaMemsetAsync(rho, 0, sizeof(float) * G, s);
+    if (N > 0)
+        pbf::k_grid_density<<<pbf::blocks_for(N, pbf::kBS), pbf::kBS, 0, s>>>(S.devicePositions(),
+                                                                            S.buffers().d_params, N, gd, rho);
+    pbf::k_grid_residual<<<nb, pbf::kBS, 0, s>>>(rho, d_target, G, partial);
+    if (d_pos_bar && N > 0)
+        pbf::k_grid_loss_grad<<<pbf::blocks_for(N, pbf::kBS), pbf::kBS, 0, s>>>(
+            S.devicePositions(), S.buffers().d_params, N, gd, rho, 2.0f / float(G), d_pos_bar);
+    std::vector<double> hp(nb);
+    cudaMemcpyAsync(hp.data(), partial, sizeof(double) * nb, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(rho, s);
+    cudaFreeAsync(partial, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return pbf::status_of(e);
+    double acc = 0.0;
+    for (double v : hp) acc += v;
+    if (loss) *loss = acc / double(G);
+    return PBF_OK;
+}
+
+}  // extern "C"

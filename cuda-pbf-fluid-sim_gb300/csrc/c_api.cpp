@@ -15,9 +15,7 @@
 #include "phases.cuh"
 #include "sort.cuh"
 
-struct pbf_sim {
-    sim::Simulator sim;
-};
+#include "handle.h"
 
 namespace {
 

@@ -151,6 +151,11 @@ _SIGS = {
                           C.POINTER(_I)], _I),
     "pbf_launches_per_step": ([_VP], _I),
     "pbf_set_neighbour_list_capacity": ([_VP, _U32], _I),
+    "pbf_forward": ([_VP, _I, _I, C.POINTER(_VP)], _I),
+    "pbf_backward": ([_VP, _VP, _VP, _VP, _VP, C.POINTER(_F)], _I),
+    "pbf_tape_destroy": ([_VP], _I),
+    "pbf_density_grid": ([_VP, _I, _VP], _I),
+    "pbf_density_grid_loss": ([_VP, _I, _VP, C.POINTER(C.c_double), _VP], _I),
     "pbf_ensemble_create": ([C.POINTER(SimParams), _U32, C.POINTER(_VP)], _I),
     "pbf_ensemble_destroy": ([_VP], _I),
     "pbf_ensemble_stream": ([_VP], _VP),

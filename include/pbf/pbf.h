@@ -299,6 +299,32 @@ int pbf_ensemble_step_host(pbf_ensemble* ens, float4* pos, float4* vel);
 int pbf_ensemble_synchronize(pbf_ensemble* ens);
 int pbf_ensemble_launches_per_step(pbf_ensemble* ens);
 
+/* ----------------------------------------------------------------- adjoint */
+/* Reverse-mode gradients of the step.  No counterpart in the reference.
+ * pbf_forward advances the handle's scene `steps` steps (its current
+ * parameters) and records (pos, vel) checkpoints every `checkpoint_every`
+ * steps in a tape.  pbf_backward takes dL/d(final positions) and dL/d(final
+ * velocities) (device float4[N], particle order, w ignored) and writes
+ * dL/d(initial positions), dL/d(initial velocities) (device float4[N], may
+ * be NULL) and dL/d(xsph_c) (host).  It replays each checkpoint segment once,
+ * recording every step's intermediates, and differentiates the steps in
+ * reverse, with each step's neighbour sets held fixed and clamps passing the
+ * derivative of the branch taken.  Device memory: 32 bytes per particle per
+ * checkpoint plus (16 (iters + 3) + 12) bytes per particle and the cell table
+ * per step of a segment.  PBF_ERR_UNSUPPORTED for XPBD (xpbd_enable). */
+typedef struct pbf_tape pbf_tape;
+int pbf_forward(pbf_sim* sim, int steps, int checkpoint_every, pbf_tape** tape);
+int pbf_backward(pbf_tape* tape, const float4* d_pos_bar, const float4* d_vel_bar, float4* d_pos0_bar,
+                 float4* d_vel0_bar, float* xsph_c_bar);
+int pbf_tape_destroy(pbf_tape* tape);
+/* SPH density of the handle's state on res^3 cell centres of its grid box:
+ * rho(g) = sum_i m W_poly6(|g - p_i|), into device float[res^3]. */
+int pbf_density_grid(pbf_sim* sim, int res, float* d_grid);
+/* loss = mean over the res^3 points of (rho(g) - target(g))^2 (target:
+ * device float[res^3]); d_pos_bar (device float4[N], may be NULL) receives
+ * dL/d(positions). */
+int pbf_density_grid_loss(pbf_sim* sim, int res, const float* d_target, double* loss, float4* d_pos_bar);
+
 /* Inspection: evaluates the device math the neighbour kernels use on
  * device arrays: fn 0 = powf(a, b), 1 = sqrtf(a), 2 = a / b (IEEE). */
 int pbf_debug_eval_math(int fn, const float* d_a, const float* d_b, float* d_out, uint32_t n);
