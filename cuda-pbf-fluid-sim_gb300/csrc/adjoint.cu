@@ -75,61 +75,66 @@ __device__ __forceinline__ float3 jt(const Pair& q, float3 g) {
     return make_float3(q.coeff * g.x + k * q.u.x, q.coeff * g.y + k * q.u.y, q.coeff * g.z + k * q.u.z);
 }
 
-// Candidates of slot s: stencil rows of its start-of-step cell.
+// The neighbour candidates of a recorded step: the step's neighbour list
+// (32-bit slots, walk order, built at the step's prediction with a radius
+// covering all its passes) or, where a list overflowed or none was kept, the
+// stencil rows of the start-of-step cell.
+struct Cand {
+    const uint32_t* __restrict__ key_s;
+    const uint32_t* __restrict__ lb;
+    const uint32_t* __restrict__ list;   // may be null
+    const uint32_t* __restrict__ count;
+    uint32_t cap;
+};
+
 template <class Visit>
-__device__ __forceinline__ void for_candidates(uint32_t s, const uint32_t* __restrict__ key_s,
-                                               const uint32_t* __restrict__ lb, const sim::DeviceParams& dp,
+__device__ __forceinline__ void for_candidates(uint32_t s, const Cand& c, const sim::DeviceParams& dp,
                                                Visit&& visit) {
+    if (c.list) {
+        const uint32_t n = c.count[s];
+        if (n <= c.cap) {
+            const uint32_t* l = c.list + size_t(s) * c.cap;
+            for (uint32_t e = 0; e < n; ++e)
+                if (!visit(__ldg(l + e))) return;
+            return;
+        }
+    }
     int cx, cy, cz;
-    decode_key(key_s[s], dp.grid.dim, cx, cy, cz);
-    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{lb}, visit);
+    decode_key(c.key_s[s], dp.grid.dim, cx, cy, cz);
+    walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{c.lb}, visit);
 }
 
 // ---------------------------------------------------------------- XSPH
 // v''_i = v_i + c g (m / rho0) sum_j (v_j - v_i) W_ij at the solved positions.
 __global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ xf, const float4* __restrict__ vf,
-                                                     const uint32_t* __restrict__ key_s,
-                                                     const uint32_t* __restrict__ lb,
-                                                     const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                     const float4* __restrict__ vbar_out, float4* __restrict__ vfbar,
-                                                     float4* __restrict__ xfbar, float* __restrict__ cbar) {
+                                                     Cand cand, const sim::DeviceParams* __restrict__ dpp,
+                                                     uint32_t N, const float4* __restrict__ vbar_out,
+                                                     float4* __restrict__ vfbar, float4* __restrict__ xfbar,
+                                                     float* __restrict__ cbar) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     float cpart = 0.f;
     if (s < N) {
         const sim::DeviceParams& dp = *dpp;
         const float4 xi = xf[s], vi = vf[s];
         const float3 g = f3(vbar_out[s]);
-        // forward: count and sum, for the gate and dL/dc
-        int count = 0;
-        float wsum = 0.f;
-        float3 sum = make_float3(0.f, 0.f, 0.f);
-        for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
-            if (k == s) return true;
-            float rx, ry, rz;
-            const float r2 = dist2(xi, xf[k], rx, ry, rz);
-            if (r2 > dp.kernel.h2) return true;
-            const float hr2 = sub_(dp.kernel.h2, r2);
-            const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
-            const float4 vj = vf[k];
-            sum.x += (vj.x - vi.x) * w;
-            sum.y += (vj.y - vi.y) * w;
-            sum.z += (vj.z - vi.z) * w;
-            wsum += w;
-            ++count;
-            return true;
-        });
         float gate = 1.0f;
-        if (dp.pbf.xsph_gate_enable) {
+        if (dp.pbf.xsph_gate_enable) {  // the gate counts neighbours first
+            int count = 0;
+            for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
+                float rx, ry, rz;
+                if (k != s && !(dist2(xi, xf[k], rx, ry, rz) > dp.kernel.h2)) ++count;
+                return true;
+            });
             const int nMin = max(0, dp.pbf.xsph_n_min);
             const int nMax = max(nMin + 1, dp.pbf.xsph_n_max);
             gate = fminf(1.f, fmaxf(0.f, (float(count) - float(nMin)) / float(nMax - nMin)));
         }
         const float mor = (dp.restDensity > 0.f) ? dp.particleMass / dp.restDensity : 0.f;
         const float ceff = dp.xsph_c * gate * mor;
-        cpart = gate * mor * dot3(sum, g);
-        atomic_add3(vfbar + s, make_float3(g.x - ceff * wsum * g.x, g.y - ceff * wsum * g.y, g.z - ceff * wsum * g.z));
+        float wsum = 0.f;
+        float3 sum = make_float3(0.f, 0.f, 0.f);
         float3 own = make_float3(0.f, 0.f, 0.f);
-        for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+        for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
             if (k == s) return true;
             float rx, ry, rz;
             const float r2 = dist2(xi, xf[k], rx, ry, rz);
@@ -137,9 +142,13 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ 
             const float hr2 = sub_(dp.kernel.h2, r2);
             const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
             const float4 vj = vf[k];
+            const float3 dv = make_float3(vj.x - vi.x, vj.y - vi.y, vj.z - vi.z);
+            sum.x += dv.x * w;
+            sum.y += dv.y * w;
+            sum.z += dv.z * w;
+            wsum += w;
             atomic_add3(vfbar + k, make_float3(ceff * w * g.x, ceff * w * g.y, ceff * w * g.z));
-            const float wbar = ceff * ((vj.x - vi.x) * g.x + (vj.y - vi.y) * g.y + (vj.z - vi.z) * g.z);
-            const float r2bar = wbar * (-3.0f * dp.kernel.poly6 * hr2 * hr2);
+            const float r2bar = ceff * dot3(dv, g) * (-3.0f * dp.kernel.poly6 * hr2 * hr2);
             const float3 ub = make_float3(2.f * rx * r2bar, 2.f * ry * r2bar, 2.f * rz * r2bar);
             own.x += ub.x;
             own.y += ub.y;
@@ -147,6 +156,8 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ 
             atomic_add3(xfbar + k, make_float3(-ub.x, -ub.y, -ub.z));
             return true;
         });
+        cpart = gate * mor * dot3(sum, g);
+        atomic_add3(vfbar + s, make_float3(g.x - ceff * wsum * g.x, g.y - ceff * wsum * g.y, g.z - ceff * wsum * g.z));
         atomic_add3(xfbar + s, own);
     }
     // dL/dc: block sum, one atomic per block
@@ -189,9 +200,7 @@ __global__ void __launch_bounds__(kBS) k_adj_velocity(const float4* __restrict__
 // ----------------------------------------------------------------- delta
 // x^{k+1}_i = x^k_i + clampDisp(relax / rho0 * sum_j (l_i + l_j + scorr_ij) a_ij)
 __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__ x, const float* __restrict__ lam,
-                                                      const uint32_t* __restrict__ key_s,
-                                                      const uint32_t* __restrict__ lb,
-                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                      Cand cand, const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                       const float4* __restrict__ xbar_in,
                                                       float4* __restrict__ xbar_out, float* __restrict__ lambar) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -204,7 +213,7 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
     const float3 gin = f3(xbar_in[s]);
     // forward displacement, for the clamp
     float3 D = make_float3(0.f, 0.f, 0.f);
-    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
         if (k == s) return true;
         float rx, ry, rz;
         const float r2 = dist2(xi, x[k], rx, ry, rz);
@@ -230,7 +239,7 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
     float lown = 0.f;
     float3 own = gin;  // identity path x^k -> x^{k+1}
     const float kcorr = pbf.scorr_k, ncorr = pbf.scorr_n;
-    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
         if (k == s) return true;
         const Pair q = pair_of(xi, x[k], dp);
         if (q.r2 > dp.kernel.h2) return true;
@@ -267,9 +276,7 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
 
 // ---------------------------------------------------------------- lambda
 // lambda_i = -(rho_i / rho0 - 1) / (scale^2 (sum_j |a_ij|^2 + |sum_j a_ij|^2) + eps)
-__global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict__ x,
-                                                       const uint32_t* __restrict__ key_s,
-                                                       const uint32_t* __restrict__ lb,
+__global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict__ x, Cand cand,
                                                        const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                        const float* __restrict__ lambar,
                                                        float4* __restrict__ xbar_out) {
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict_
     const float4 xi = x[s];
     const int cap = dp.maxNeighbors > 0 ? dp.maxNeighbors : 0x7FFFFFFF;
     LambdaAcc acc;
-    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
         if (acc.contrib >= cap) return false;
         if (k == s) return true;
         float rx, ry, rz;
@@ -311,7 +318,7 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict_
     const float3 G = make_float3(acc.gx, acc.gy, acc.gz);
     float3 own = make_float3(0.f, 0.f, 0.f);
     int seen = 0;
-    for_candidates(s, key_s, lb, dp, [&](uint32_t k) -> bool {
+    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
         if (seen >= cap) return false;
         if (k == s) return true;
         const Pair q = pair_of(xi, x[k], dp);
@@ -487,6 +494,8 @@ struct StepRecord {
     uint32_t* key_s = nullptr;
     uint32_t* perm = nullptr;
     uint32_t* lb = nullptr;
+    uint32_t* list = nullptr;   // the step's neighbour lists (null: none kept)
+    uint32_t* count = nullptr;
 };
 
 }  // namespace
@@ -512,6 +521,9 @@ struct pbf_tape {
     float4 *pbar = nullptr, *vbar = nullptr, *xfbar = nullptr, *vxbar = nullptr, *vfbar = nullptr, *xbA = nullptr,
            *xbB = nullptr, *pbar_s = nullptr;
     float *lambar = nullptr, *cbar = nullptr;
+    uint32_t* listStats = nullptr;
+    uint32_t listCap = 0;  // 0: the replay walks the stencil
+    int listSpan = 0;
     std::vector<void*> owned;
 
     template <class T>
@@ -534,7 +546,7 @@ struct pbf_tape {
         sh.iters = iters;
         sh.hashed = false;
         sh.xsph = xsph;
-        sh.list_span = 0;
+        sh.list_span = listCap ? listSpan : 0;
         return sh;
     }
 
@@ -558,10 +570,17 @@ struct pbf_tape {
         b.sort_bytes = sortBytes;
         b.dp = dp;
         b.err = err;
+        b.nbr_list = r.list;
+        b.nbr_count = r.count;
+        b.nbr_stats = listStats;
+        b.nbr_cap = r.list ? listCap : 0u;
+        b.nbr_staging = false;
         cudaError_t e;
         if ((e = fused_predict_keys(b, sh, stream)) != cudaSuccess) return e;
         if ((e = fused_sort(b, sh, stream)) != cudaSuccess) return e;
         if ((e = fused_gather_and_tables(b, sh, stream)) != cudaSuccess) return e;
+        e = fused_build_lists(b, sh, 0, stream);
+        if (e != cudaSuccess && e != cudaErrorNotReady) return e;
         if (iters <= 0) {
             if ((e = fused_solve(b, sh, stream)) != cudaSuccess) return e;  // boundary + velocity on x[0]
         }
@@ -587,9 +606,10 @@ struct pbf_tape {
         const size_t b4 = sizeof(float4) * N;
         k_adj_gather_out<<<g, kBS, 0, stream>>>(r.perm, pbar, vbar, N, xfbar, vxbar);
         const float4* xf = r.x[std::max(iters, 0)];
+        const Cand cand{r.key_s, r.lb, r.list, r.count, listCap};
         if (xsph) {
             cudaMemsetAsync(vfbar, 0, b4, stream);
-            k_adj_xsph<<<ga, kAdjBS, 0, stream>>>(xf, r.vf, r.key_s, r.lb, dp, N, vxbar, vfbar, xfbar, cbar);
+            k_adj_xsph<<<ga, kAdjBS, 0, stream>>>(xf, r.vf, cand, dp, N, vxbar, vfbar, xfbar, cbar);
         } else {
             cudaMemcpyAsync(vfbar, vxbar, b4, cudaMemcpyDeviceToDevice, stream);
         }
@@ -599,8 +619,8 @@ struct pbf_tape {
         for (int it = iters - 1; it >= 0; --it) {
             cudaMemsetAsync(xout, 0, b4, stream);
             cudaMemsetAsync(lambar, 0, sizeof(float) * N, stream);
-            k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], r.key_s, r.lb, dp, N, xin, xout, lambar);
-            k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.key_s, r.lb, dp, N, lambar, xout);
+            k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], cand, dp, N, xin, xout, lambar);
+            k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], cand, dp, N, lambar, xout);
             std::swap(xin, xout);
         }
         k_adj_predict<<<g, kBS, 0, stream>>>(r.x[0], xin, pbar_s, r.perm, dp, N, pbar, vbar);
@@ -625,12 +645,26 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
     t->keyBits = bits_for(t->numCells - 1u);
     t->sortBytes = sort_temp_bytes(N, t->keyBits);
     const int segs = (steps + every - 1) / every;
+    // Keep each recorded step's neighbour lists when one list serves the
+    // whole step (the single-list schedule) and they fit in a quarter of the
+    // free device memory.
+    const int span = list_span_for(sp);
+    if (span >= sp.solverIters && span > 0) {
+        size_t freeB = 0, totalB = 0;
+        cudaMemGetInfo(&freeB, &totalB);
+        const uint32_t cap = sim::Simulator::kDefaultListCapacity;
+        const size_t need = size_t(std::min(every, steps)) * N * (size_t(cap) + 1) * sizeof(uint32_t);
+        if (need <= freeB / 4) {
+            t->listCap = cap;
+            t->listSpan = span;
+        }
+    }
     bool ok = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) == cudaSuccess && t->alloc(&t->pos, N) &&
               t->alloc(&t->vel, N) && t->alloc(&t->keys, N) && t->alloc(&t->dp, 1) && t->alloc(&t->err, 1) &&
               t->alloc(reinterpret_cast<unsigned char**>(&t->sortTemp), t->sortBytes) && t->alloc(&t->pbar, N) &&
               t->alloc(&t->vbar, N) && t->alloc(&t->xfbar, N) && t->alloc(&t->vxbar, N) && t->alloc(&t->vfbar, N) &&
               t->alloc(&t->xbA, N) && t->alloc(&t->xbB, N) && t->alloc(&t->pbar_s, N) && t->alloc(&t->lambar, N) &&
-              t->alloc(&t->cbar, 1);
+              t->alloc(&t->cbar, 1) && t->alloc(&t->listStats, 2);
     for (int c = 0; ok && c < segs; ++c) {
         float4 *cp = nullptr, *cv = nullptr;
         ok = t->alloc(&cp, N) && t->alloc(&cv, N);
@@ -646,11 +680,13 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
         for (auto& l : r.lam) ok = ok && t->alloc(&l, N);
         ok = ok && t->alloc(&r.vf, N) && t->alloc(&r.ps, N) && t->alloc(&r.key_s, N) && t->alloc(&r.perm, N) &&
              t->alloc(&r.lb, size_t(t->numCells) + 1);
+        if (ok && t->listCap) ok = t->alloc(&r.list, size_t(N) * t->listCap) && t->alloc(&r.count, N);
     }
     if (ok) {
         const sim::DeviceParams dp = sim::MakeDeviceParams(sp);
         ok = cudaMemcpy(t->dp, &dp, sizeof(dp), cudaMemcpyHostToDevice) == cudaSuccess &&
-             cudaMemset(t->err, 0, sizeof(uint32_t)) == cudaSuccess;
+             cudaMemset(t->err, 0, sizeof(uint32_t)) == cudaSuccess &&
+             cudaMemset(t->listStats, 0, 2 * sizeof(uint32_t)) == cudaSuccess && fused_prepare_kernels() == cudaSuccess;
     }
     if (!ok) {
         const cudaError_t e = cudaGetLastError();

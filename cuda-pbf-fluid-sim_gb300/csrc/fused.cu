@@ -61,6 +61,7 @@ struct ListArgs {
     const uint32_t* __restrict__ count;
     uint32_t cap;
     int updates;
+    int staging;  // 0: no tile is staged (all lists hold 32-bit slots)
 };
 
 // ------------------------------------------------------------- tiles
@@ -208,7 +209,8 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                                                           const uint32_t* __restrict__ lb,
                                                           const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                           int updates, uint32_t cap, uint32_t* __restrict__ list,
-                                                          uint32_t* __restrict__ count, uint32_t* __restrict__ stats) {
+                                                          uint32_t* __restrict__ count, uint32_t* __restrict__ stats,
+                                                          int staging) {
     const sim::DeviceParams& dp = *dpp;
     float R2;
     if (!list_radius2(dp, updates, R2)) return;
@@ -216,7 +218,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     const uint32_t s0 = (blockIdx.x * kBuildBS + threadIdx.x) & ~31u;
     if (s0 >= N) return;  // warp-uniform
     const WarpPlan plan = plan_tile_warp(key_s, lb, dp, s0 - s0 % uint32_t(kTile), N);
-    const bool staged = plan.staged;
+    const bool staged = plan.staged && staging;
     const uint32_t planShift = plan.base - plan.start;  // lane r: stage index of slot k in row r is k + shift
     const int reach = neighbour_reach(dp);
     const int side = 2 * reach + 1;
@@ -313,10 +315,10 @@ __global__ void __launch_bounds__(kTile) k_lambda(const float4* __restrict__ pre
     if (lists) {
         if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
         __syncthreads();
-        if (P.staged) stage_tile(P, pred, nullptr, nullptr, sp, nullptr);
+        if (P.staged && la.staging) stage_tile(P, pred, nullptr, nullptr, sp, nullptr);
         __syncthreads();
     }
-    const bool staged = lists && P.staged;
+    const bool staged = lists && P.staged && la.staging;
     const float4 pi = pred[sc];
     const GlobalData g{pred, nullptr, nullptr};
     uint32_t n;
@@ -363,10 +365,10 @@ __global__ void __launch_bounds__(kTile) k_delta(const float4* __restrict__ pred
     if (lists) {
         if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
         __syncthreads();
-        if (P.staged) stage_tile(P, pred, lam, nullptr, sp, nullptr);
+        if (P.staged && la.staging) stage_tile(P, pred, lam, nullptr, sp, nullptr);
         __syncthreads();
     }
-    const bool staged = lists && P.staged;
+    const bool staged = lists && P.staged && la.staging;
     const float4 pi = pred[sc];
     const float lam_i = lam[sc];
     const float w_q = scorr_wq(dp);
@@ -448,10 +450,10 @@ __global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pre
         if (lists) {
             if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
             __syncthreads();
-            if (P.staged) stage_tile(P, pred, nullptr, vel_s, sp, sv);
+            if (P.staged && la.staging) stage_tile(P, pred, nullptr, vel_s, sp, sv);
             __syncthreads();
         }
-        const bool staged = lists && P.staged;
+        const bool staged = lists && P.staged && la.staging;
         // Queue of the queued walks: the stage area, free in tiles that are
         // not staged.  In a staged tile a warp whose lists overflowed walks
         // the stencil without a queue.
@@ -647,7 +649,7 @@ int list_updates(const FusedShape& sh, int it) {
 }
 
 ListArgs list_args(const FusedBufs& b, const FusedShape& sh, int it) {
-    ListArgs la{b.nbr_list, b.nbr_count, b.nbr_cap, -1};
+    ListArgs la{b.nbr_list, b.nbr_count, b.nbr_cap, -1, b.nbr_staging ? 1 : 0};
     if (lists_on(b, sh)) la.updates = list_updates(sh, it);
     return la;
 }
@@ -689,7 +691,7 @@ cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, 
     const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
     k_build_lists<<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(cur, b.key_s, b.lb, b.dp, sh.N,
                                                                  list_updates(sh, it), b.nbr_cap, b.nbr_list,
-                                                                 b.nbr_count, b.nbr_stats);
+                                                                 b.nbr_count, b.nbr_stats, b.nbr_staging ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,9 @@ struct FusedBufs {
     uint32_t* nbr_count;
     uint32_t* nbr_stats;
     uint32_t nbr_cap;  // entries per particle, a multiple of 8; 0 = no lists
+    // false: every list holds 32-bit sorted slots (no tile is staged), for
+    // lists that are read outside the list passes (the adjoint)
+    bool nbr_staging = true;
 };
 
 struct FusedShape {
