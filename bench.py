@@ -571,7 +571,7 @@ def run_ensemble(args, cfg, world, rank, local):
     # Looped: every scene its own pbf_sim, stepped scene after scene from the
     # same post-warm-up state (each handle on its own stream, so neighbouring
     # scenes' launches may overlap on the GPU).
-    loop_steps = max(1, min(args.steps, args.loop_steps))
+    loop_steps = args.steps if args.loop_steps <= 0 else max(1, min(args.steps, args.loop_steps))
     off = np.zeros(S + 1, np.int64)
     off[1:] = np.cumsum([p.numParticles for p in scenes])
     sims = []
@@ -592,9 +592,22 @@ def run_ensemble(args, cfg, world, rank, local):
     for sm in sims:
         pbfx.check(lib.pbf_synchronize(sm.h))
     loop_s = time.perf_counter() - t0
+    # Serial: one scene-step at a time, each completed before the next (a
+    # single simulator stepping the scenes in turn).
+    serial_steps = max(1, min(loop_steps, 5))
+    for k, sm in enumerate(sims):
+        sm.upload(snap_pos[off[k]:off[k + 1]], snap_vel[off[k]:off[k + 1]])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(serial_steps):
+        for sm in sims:
+            lib.pbf_step(sm.h, None)
+            pbfx.check(lib.pbf_synchronize(sm.h))
+    serial_s = time.perf_counter() - t0
     for sm in sims:
         sm.close()
     looped = S * loop_steps / loop_s
+    looped_serial = S * serial_steps / serial_s
 
     line = {
         "metric": "scene-steps/s (ensemble of 256 scenes)", "value": value, "unit": "scene-steps/s", "n_gpus": world,
@@ -610,9 +623,14 @@ def run_ensemble(args, cfg, world, rank, local):
                    "l2": "flushed before every timed step (256 MiB write, untimed)"},
         "particle_steps_per_s": n * args.steps / total_s,
         "looped": {"value": looped, "unit": "scene-steps/s", "steps": loop_steps,
-                   "what": "each scene its own pbf_sim (fused step, one graph per scene-step), host loop over "
-                           "scenes, same post-warm-up state, wall clock",
+                   "what": "each scene its own pbf_sim (fused step, one graph per scene-step, one stream per "
+                           "scene so scenes overlap on the GPU), host loop over scenes, same post-warm-up state, "
+                           "wall clock",
                    "speedup_of_ensemble": value / looped},
+        "looped_serial": {"value": looped_serial, "unit": "scene-steps/s", "steps": serial_steps,
+                          "what": "the same pbf_sims stepped one scene at a time, each step completed before the "
+                                  "next, from the same state, wall clock",
+                          "speedup_of_ensemble": value / looped_serial},
         "e2e": {"value": S * e2e_steps / e2e_s, "unit": "scene-steps/s", "h2d_bytes_per_step": 32 * n,
                 "d2h_bytes_per_step": 32 * n, "steps": e2e_steps,
                 "api": "pbf_ensemble_step_host (pinned host pos/vel in, one step, pos/vel out)"},
@@ -661,7 +679,8 @@ def main(argv=None):
     ap.add_argument("--ref-budget", type=float, default=150.0, help="seconds cap of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
-    ap.add_argument("--loop-steps", type=int, default=10, help="steps of the looped baseline (c4)")
+    ap.add_argument("--loop-steps", type=int, default=0,
+                    help="steps of the looped baseline (c4); 0 = the timed steps, the same window as the ensemble")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

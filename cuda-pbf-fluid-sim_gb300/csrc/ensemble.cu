@@ -12,6 +12,10 @@
 //   * each particle reads its scene's parameter block (grid, gravity, dt,
 //     kernel, tuning, iteration count); a warp may hold particles of two
 //     scenes, which the per-lane walks allow;
+//   * the neighbour passes are the simulator's own list kernels with a
+//     per-slot scene lookup (fused.cu): lists built once per step for the
+//     scenes whose single-list schedule holds, tiles of one scene row staged
+//     in shared memory;
 //   * scenes with fewer solver iterations than the ensemble's maximum carry
 //     their prediction through the remaining passes unchanged.
 // Every scene therefore evolves bit-identically to a pbf_sim of the same
@@ -23,6 +27,8 @@
 #include <vector>
 
 #include "../../include/pbf/pbf.h"
+#include "../../include/pbf/simulator.h"
+#include "fused.cuh"
 #include "grid.cuh"
 #include "pbf_common.cuh"
 #include "sort.cuh"
@@ -31,15 +37,6 @@ namespace pbf {
 namespace {
 
 constexpr int kBS = 256;
-constexpr int kEnsBS = 128;
-constexpr int kEnsQueue = 32;
-
-struct SceneInfo {
-    sim::DeviceParams dp;
-    uint32_t cellOffset;
-    int iters;
-};
-
 __global__ void __launch_bounds__(kBS) k_ens_predict_keys(const float4* __restrict__ pos, const float4* __restrict__ vel,
                                                           const SceneInfo* __restrict__ scenes,
                                                           const uint32_t* __restrict__ sceneOfId, uint32_t N,
@@ -65,95 +62,6 @@ __global__ void __launch_bounds__(kBS) k_ens_gather(const uint32_t* __restrict__
     pred_s[s] = predict_clamped(p, vel[i], scenes[sc].dp.gravity, scenes[sc].dp.dt, scenes[sc].dp.grid);
     pos_s[s] = p;
     sceneOfSlot[s] = sc;
-}
-
-// Stencil rows of slot s in its scene's cell range.
-__device__ __forceinline__ RowSource scene_rows(const SceneInfo& sc, uint32_t key, const uint32_t* __restrict__ lb) {
-    RowSource r;
-    decode_key(key - sc.cellOffset, sc.dp.grid.dim, r.cx, r.cy, r.cz);
-    r.reach = neighbour_reach(sc.dp);
-    r.dim = sc.dp.grid.dim;
-    r.lb = lb + sc.cellOffset;
-    return r;
-}
-
-__global__ void __launch_bounds__(kEnsBS) k_ens_lambda(int it, const float4* __restrict__ pred,
-                                                       const uint32_t* __restrict__ key_s,
-                                                       const uint32_t* __restrict__ lb,
-                                                       const SceneInfo* __restrict__ scenes,
-                                                       const uint32_t* __restrict__ sceneOfSlot, uint32_t N,
-                                                       float* __restrict__ lam) {
-    __shared__ uint32_t s_queue[kEnsQueue * kEnsBS];
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t sc = s < N ? s : 0u;
-    const SceneInfo& scene = scenes[sceneOfSlot[sc]];
-    const bool active = s < N && it < scene.iters;  // every lane takes part in the warp-wide rounds
-    const float l = lambda_queued<kEnsQueue, kEnsBS>(active, sc, pred[sc], scene_rows(scene, key_s[sc], lb), scene.dp,
-                                                     GlobalData{pred, nullptr, nullptr}, s_queue + threadIdx.x);
-    if (active) lam[s] = l;
-}
-
-__global__ void __launch_bounds__(kEnsBS) k_ens_delta(int it, const float4* __restrict__ pred,
-                                                      const float* __restrict__ lam,
-                                                      const uint32_t* __restrict__ key_s,
-                                                      const uint32_t* __restrict__ lb,
-                                                      const SceneInfo* __restrict__ scenes,
-                                                      const uint32_t* __restrict__ sceneOfSlot, uint32_t N,
-                                                      float4* __restrict__ pred_out,
-                                                      const float4* __restrict__ pos_s, float4* __restrict__ vel_s) {
-    __shared__ uint32_t s_queue[kEnsQueue * kEnsBS];
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t sc = s < N ? s : 0u;
-    const SceneInfo& scene = scenes[sceneOfSlot[sc]];
-    const sim::DeviceParams& dp = scene.dp;
-    const bool solve = s < N && it < scene.iters;
-    const float4 pi = pred[sc];
-    const float3 d = delta_queued<kEnsQueue, kEnsBS>(solve, sc, pi, lam[sc], scene_rows(scene, key_s[sc], lb), dp,
-                                                     scorr_wq(dp), GlobalData{pred, lam, nullptr},
-                                                     s_queue + threadIdx.x);
-    if (s >= N) return;
-    // A scene past its iterations carries its prediction through; a scene
-    // without iterations applies boundary and velocity to it in pass 0.
-    const bool last = solve ? it == scene.iters - 1 : (scene.iters <= 0 && it == 0);
-    float4 x = solve ? make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w) : pi;
-    if (last) {
-        // Boundary(e=0) after the solve loop (sim/phases.cpp:94) and the
-        // velocity phase (sim/phases.cpp:102-105).
-        float4 vdummy = make_float4(0.f, 0.f, 0.f, 0.f);
-        boundary_apply(x, vdummy, dp.grid, 0.0f);
-        const float inv_dt = div_(1.0f, dp.dt);
-        const float4 p = pos_s[s];
-        vel_s[s] = make_float4(mul_(sub_(x.x, p.x), inv_dt), mul_(sub_(x.y, p.y), inv_dt),
-                               mul_(sub_(x.z, p.z), inv_dt), 0.0f);
-    }
-    pred_out[s] = x;
-}
-
-__global__ void __launch_bounds__(kEnsBS) k_ens_commit(const float4* __restrict__ pred,
-                                                       const float4* __restrict__ vel_s,
-                                                       const uint32_t* __restrict__ key_s,
-                                                       const uint32_t* __restrict__ lb,
-                                                       const uint32_t* __restrict__ perm,
-                                                       const SceneInfo* __restrict__ scenes,
-                                                       const uint32_t* __restrict__ sceneOfSlot, uint32_t N,
-                                                       float4* __restrict__ pos, float4* __restrict__ vel) {
-    __shared__ uint32_t s_queue[kEnsQueue * kEnsBS];
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t sc = s < N ? s : 0u;
-    const SceneInfo& scene = scenes[sceneOfSlot[sc]];
-    const sim::DeviceParams& dp = scene.dp;
-    float4 x = pred[sc];
-    float4 v = vel_s[sc];
-    // XSPH where the scene configures it (sim/simulator.cpp:277-285)
-    const bool xsph = s < N && dp.xsph_c > 0.f;
-    const float4 vx = xsph_queued<kEnsQueue, kEnsBS>(xsph, sc, x, v, scene_rows(scene, key_s[sc], lb), dp,
-                                                     GlobalData{pred, nullptr, vel_s}, s_queue + threadIdx.x);
-    if (s >= N) return;
-    if (xsph) v = vx;
-    boundary_apply(x, v, dp.grid, dp.boundaryRestitution);
-    const uint32_t i = perm[s];
-    pos[i] = x;
-    vel[i] = v;
 }
 
 template <class T>
@@ -188,7 +96,8 @@ struct pbf_ensemble {
     float4 *pos = nullptr, *vel = nullptr, *pred_a = nullptr, *pred_b = nullptr, *pos_s = nullptr, *vel_s = nullptr;
     float* lam = nullptr;
     uint32_t *keys = nullptr, *key_s = nullptr, *perm = nullptr, *lb = nullptr, *sceneOfId = nullptr,
-             *sceneOfSlot = nullptr, *err = nullptr;
+             *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr;
+    uint32_t nbrCap = 0;
     pbf::SceneInfo* scenes = nullptr;
     void* sortTemp = nullptr;
     size_t sortBytes = 0;
@@ -201,33 +110,52 @@ struct pbf_ensemble {
         if (graph) cudaGraphDestroy(graph);
         for (void* p : {(void*)pos, (void*)vel, (void*)pred_a, (void*)pred_b, (void*)pos_s, (void*)vel_s, (void*)lam,
                         (void*)keys, (void*)key_s, (void*)perm, (void*)lb, (void*)sceneOfId, (void*)sceneOfSlot,
-                        (void*)err, (void*)scenes, sortTemp})
+                        (void*)err, (void*)scenes, sortTemp, (void*)nbrList, (void*)nbrCount, (void*)nbrStats})
             if (p) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
     }
 
     float4* final_pred() const { return (passes % 2 == 0) ? pred_a : pred_b; }
 
+    pbf::MultiBufs bufs() const {
+        pbf::MultiBufs m{};
+        m.N = N;
+        m.scenes = scenes;
+        m.sceneOfSlot = sceneOfSlot;
+        m.pos = pos;
+        m.vel = vel;
+        m.pred_a = pred_a;
+        m.pred_b = pred_b;
+        m.pos_s = pos_s;
+        m.vel_s = vel_s;
+        m.lam_s = lam;
+        m.key_s = key_s;
+        m.perm = perm;
+        m.lb = lb;
+        m.nbr_list = nbrList;
+        m.nbr_count = nbrCount;
+        m.nbr_stats = nbrStats;
+        m.nbr_cap = nbrCap;
+        return m;
+    }
+
     // The step as launches on `stream` (captured once into the graph).
     cudaError_t enqueue() {
         using namespace pbf;
         if (N == 0) return cudaSuccess;
-        const unsigned g = blocks_for(N, kBS), gn = blocks_for(N, kEnsBS);
+        const unsigned g = blocks_for(N, kBS);
         k_ens_predict_keys<<<g, kBS, 0, stream>>>(pos, vel, scenes, sceneOfId, N, keys);
         cudaError_t e = sort_pairs(sortTemp, sortBytes, keys, key_s, nullptr, perm, N, keyBits, stream, err);
         if (e != cudaSuccess) return e;
         k_ens_gather<<<g, kBS, 0, stream>>>(perm, pos, vel, scenes, sceneOfId, N, pred_a, pos_s, sceneOfSlot);
         if ((e = launch_cell_lb(lb, key_s, N, totalCells, stream)) != cudaSuccess) return e;
+        const MultiBufs m = bufs();
+        if ((e = multi_build_lists(m, stream)) != cudaSuccess) return e;
         for (int it = 0; it < passes; ++it) {
-            float4* cur = (it % 2 == 0) ? pred_a : pred_b;
-            float4* nxt = (it % 2 == 0) ? pred_b : pred_a;
-            k_ens_lambda<<<gn, kEnsBS, 0, stream>>>(it, cur, key_s, lb, scenes, sceneOfSlot, N, lam);
-            k_ens_delta<<<gn, kEnsBS, 0, stream>>>(it, cur, lam, key_s, lb, scenes, sceneOfSlot, N, nxt, pos_s,
-                                                   vel_s);
+            if ((e = multi_solve_phase(m, it, 0, stream)) != cudaSuccess) return e;
+            if ((e = multi_solve_phase(m, it, 1, stream)) != cudaSuccess) return e;
         }
-        k_ens_commit<<<gn, kEnsBS, 0, stream>>>(final_pred(), vel_s, key_s, lb, perm, scenes, sceneOfSlot, N, pos,
-                                                vel);
-        return cudaGetLastError();
+        return multi_commit(m, final_pred(), stream);
     }
 
     int capture() {
@@ -272,6 +200,9 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
         info[s].dp = sim::MakeDeviceParams(p);
         info[s].cellOffset = uint32_t(cells);
         info[s].iters = p.solverIters;
+        // one list per step where the simulator's schedule builds one
+        const int span = list_span_for(p);
+        info[s].listUpdates = (span > 0 && span >= p.solverIters) ? p.solverIters : -1;
         offsets[s] = uint32_t(n);
         n += p.numParticles;
         cells += nc;
@@ -297,7 +228,19 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
               dalloc(&e->vel_s, N) && dalloc(&e->lam, N) && dalloc(&e->keys, N) && dalloc(&e->key_s, N) &&
               dalloc(&e->perm, N) && dalloc(&e->lb, size_t(e->totalCells) + 1) && dalloc(&e->sceneOfId, N) &&
               dalloc(&e->sceneOfSlot, N) && dalloc(&e->err, 1) && dalloc(&e->scenes, num_scenes) &&
-              cudaMalloc(&e->sortTemp, e->sortBytes) == cudaSuccess;
+              cudaMalloc(&e->sortTemp, e->sortBytes) == cudaSuccess && dalloc(&e->nbrStats, 2) &&
+              fused_prepare_kernels() == cudaSuccess;
+    if (ok) {  // neighbour lists: optional (without them every scene walks the stencil)
+        const uint32_t cap = sim::Simulator::kDefaultListCapacity;
+        if (dalloc(&e->nbrList, size_t(N) * cap) && dalloc(&e->nbrCount, N)) {
+            e->nbrCap = cap;
+        } else {
+            cudaGetLastError();
+            if (e->nbrList) cudaFree(e->nbrList);
+            e->nbrList = nullptr;
+        }
+        cudaMemset(e->nbrStats, 0, 2 * sizeof(uint32_t));
+    }
     if (ok) {
         ok = cudaMemcpy(e->scenes, info.data(), sizeof(SceneInfo) * num_scenes, cudaMemcpyHostToDevice) ==
                  cudaSuccess &&
@@ -386,7 +329,8 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
 int pbf_ensemble_launches_per_step(pbf_ensemble* e) {
     if (!e) return 0;
     const int sortPasses = (e->keyBits + 7) / 8;
-    return 1 /*predict_keys*/ + 1 /*hist*/ + sortPasses + 1 /*gather*/ + 1 /*lb*/ + 2 * e->passes + 1 /*commit*/;
+    return 1 /*predict_keys*/ + 1 /*hist*/ + sortPasses + 1 /*gather*/ + 1 /*lb*/ + (e->nbrCap ? 1 : 0) /*lists*/ +
+           2 * e->passes + 1 /*commit*/;
 }
 
 }  // extern "C"

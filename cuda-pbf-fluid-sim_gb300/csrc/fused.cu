@@ -54,28 +54,64 @@ __global__ void __launch_bounds__(kBS) k_gather(const uint32_t* __restrict__ per
     pos_s[s] = p;
 }
 
-// Neighbour lists of one pass: the list built for the span this pass belongs
-// to (updates = position updates it covers; < 0: no list this pass).
-struct ListArgs {
+// ------------------------------------------------------------- scenes
+// The list kernels serve one scene (the simulator) or many (the batched
+// ensemble) through a scene policy: view(s) gives the parameters of the
+// scene sorted slot s belongs to, the first cell of that scene in the global
+// cell numbering (keys are global: scene cells are numbered consecutively),
+// its solver iteration count and the position updates its neighbour lists
+// cover in this pass (< 0: that scene walks the stencil).
+struct SceneView {
+    const sim::DeviceParams* dp;
+    uint32_t cellOffset;
+    int iters;
+    int listUpdates;
+};
+
+struct OneScene {
+    const sim::DeviceParams* dp;
+    int iters;
+    int listUpdates;
+    __device__ __forceinline__ uint32_t id(uint32_t) const { return 0u; }
+    __device__ __forceinline__ SceneView view(uint32_t) const { return SceneView{dp, 0u, iters, listUpdates}; }
+};
+
+struct ManyScenes {
+    const SceneInfo* __restrict__ scenes;
+    const uint32_t* __restrict__ sceneOfSlot;
+    __device__ __forceinline__ uint32_t id(uint32_t s) const { return sceneOfSlot[s]; }
+    __device__ __forceinline__ SceneView view(uint32_t s) const {
+        const SceneInfo& si = scenes[sceneOfSlot[s]];
+        return SceneView{&si.dp, si.cellOffset, si.iters, si.listUpdates};
+    }
+};
+
+// Neighbour-list buffers of a pass.
+struct ListBufs {
     const uint32_t* __restrict__ list;
     const uint32_t* __restrict__ count;
-    uint32_t cap;
-    int updates;
-    int staging;  // 0: no tile is staged (all lists hold 32-bit slots)
+    uint32_t cap;  // 0: no lists
+    int staging;   // 0: no tile is staged (all lists hold 32-bit slots)
 };
+
+// Whether slot s's scene has lists this pass (the builder decided the same).
+__device__ __forceinline__ bool scene_lists(const SceneView& v, const ListBufs& lb) {
+    float R2;
+    return lb.cap > 0 && v.listUpdates >= 0 && list_radius2(*v.dp, v.listUpdates, R2);
+}
 
 // ------------------------------------------------------------- tiles
 // The list passes work on tiles of kTile consecutive sorted slots, one CTA
-// per tile.  When the tile's particles all lie in one (y, z) row of cells,
-// the union of their stencils is (2 reach + 1)^2 rows of cells, each one
-// contiguous slot range [start, start + len) covering the tile's x range
-// widened by reach.  If those ranges hold at most kStageMax slots, the
-// tile is "staged": every list pass copies the ranges into shared memory
-// (row r at base[r]) and the lists of its particles hold 16-bit indices
-// into that copy, so neighbour reads are shared-memory gathers.  Other tiles'
-// lists hold 32-bit sorted slots read from global memory.  The plan depends
-// only on the sorted keys, the lower-bound table and the grid, so the list
-// builder and every list pass derive the same one.
+// per tile.  When the tile's particles all lie in one scene and one (y, z)
+// row of cells, the union of their stencils is (2 reach + 1)^2 rows of
+// cells, each one contiguous slot range [start, start + len) covering the
+// tile's x range widened by reach.  If those ranges hold at most kStageMax
+// slots, the tile is "staged": every list pass copies the ranges into shared
+// memory (row r at base[r]) and the lists of its particles hold 16-bit
+// indices into that copy, so neighbour reads are shared-memory gathers.
+// Other tiles' lists hold 32-bit sorted slots read from global memory.  The
+// plan depends only on the sorted keys, the lower-bound table and the
+// scenes, so the list builder and every list pass derive the same one.
 constexpr int kTile = kNbrBS;
 constexpr int kStageMax = 1536;
 constexpr int kPlanRows = 32;
@@ -88,6 +124,7 @@ struct TilePlan {
     uint32_t total;
     int nrows;
     int staged;
+    int lists;  // the tile's scene has lists this pass
 };
 
 // A tile's plan as one warp holds it: lane r holds row r's range and stage
@@ -97,38 +134,45 @@ struct WarpPlan {
     uint32_t total;
     int nrows;
     bool staged;
+    bool lists;
 };
 
+template <class Scenes>
 __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                   const sim::DeviceParams& dp, uint32_t t0, uint32_t N) {
+                                   const Scenes& S, const ListBufs& lbuf, uint32_t t0, uint32_t N) {
     const int lane = int(threadIdx.x & 31u);
     const uint32_t tl = min(t0 + uint32_t(kTile), N) - 1u;
+    const SceneView v = S.view(t0);
+    const sim::DeviceParams& dp = *v.dp;
     const int3 dim = dp.grid.dim;
-    int xf, yf, zf, xl, yl, zl;
-    decode_key(key_s[t0], dim, xf, yf, zf);
-    decode_key(key_s[tl], dim, xl, yl, zl);
+    const bool oneScene = S.id(t0) == S.id(tl);
+    int xf, yf, zf, xl = 0, yl = -1, zl = -1;
+    decode_key(key_s[t0] - v.cellOffset, dim, xf, yf, zf);
+    if (oneScene) decode_key(key_s[tl] - v.cellOffset, dim, xl, yl, zl);
     const int reach = neighbour_reach(dp);
     const int side = 2 * reach + 1;
     WarpPlan w;
     w.nrows = side * side;
+    w.lists = scene_lists(v, lbuf);
     // sorted keys: equal (y, z) at both ends means one row for the whole tile
-    const bool single = yf == yl && zf == zl && w.nrows <= kPlanRows;
+    const bool single = oneScene && yf == yl && zf == zl && w.nrows <= kPlanRows;
     w.start = 0;
     w.len = 0;
     if (single && lane < w.nrows) {
         const int z = zf + lane / side - reach;
         const int y = yf + lane % side - reach;
         if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
+            const uint32_t* slb = lb + v.cellOffset;
             const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
-            w.start = __ldg(lb + row + uint32_t(max(xf - reach, 0)));
-            w.len = __ldg(lb + row + uint32_t(min(xl + reach, dim.x - 1)) + 1u) - w.start;
+            w.start = __ldg(slb + row + uint32_t(max(xf - reach, 0)));
+            w.len = __ldg(slb + row + uint32_t(min(xl + reach, dim.x - 1)) + 1u) - w.start;
         }
     }
     uint32_t incl = w.len;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += v;
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += t;
     }
     w.total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     w.base = incl - w.len;
@@ -137,9 +181,10 @@ __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uin
 }
 
 // The plan in shared memory for a CTA (written by warp 0).
+template <class Scenes>
 __device__ void plan_tile(TilePlan& P, const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                          const sim::DeviceParams& dp, uint32_t t0, uint32_t N) {
-    const WarpPlan w = plan_tile_warp(key_s, lb, dp, t0, N);
+                          const Scenes& S, const ListBufs& lbuf, uint32_t t0, uint32_t N) {
+    const WarpPlan w = plan_tile_warp(key_s, lb, S, lbuf, t0, N);
     const int lane = int(threadIdx.x & 31u);
     P.start[lane] = w.start;
     P.base[lane] = w.base;
@@ -148,30 +193,27 @@ __device__ void plan_tile(TilePlan& P, const uint32_t* __restrict__ key_s, const
         P.total = w.total;
         P.nrows = w.nrows;
         P.staged = w.staged ? 1 : 0;
+        P.lists = w.lists ? 1 : 0;
     }
 }
 
-// Whether this pass may use lists (the builder decided the same from the same
-// parameters); CTA-uniform.
-__device__ __forceinline__ bool lists_usable(const ListArgs& la, const sim::DeviceParams& dp) {
-    float R2;
-    return la.updates >= 0 && la.cap > 0 && list_radius2(dp, la.updates, R2);
-}
-
-// Whether this warp walks its lists: no lane's list overflowed.  Every lane
-// must call it.
-__device__ __forceinline__ bool warp_lists_fit(const ListArgs& la, bool active, uint32_t sc, uint32_t& n) {
-    n = active ? la.count[sc] : 0u;
-    return !__any_sync(0xFFFFFFFFu, n > la.cap);
+// Whether this warp walks its lists: every lane that walks has lists in its
+// scene and none of them overflowed.  Every lane must call it.
+__device__ __forceinline__ bool warp_lists_fit(const ListBufs& lbuf, bool active, bool laneLists, uint32_t sc,
+                                               uint32_t& n) {
+    n = 0;
+    if (!__all_sync(0xFFFFFFFFu, !active || laneLists)) return false;
+    n = active ? lbuf.count[sc] : 0u;
+    return !__any_sync(0xFFFFFFFFu, n > lbuf.cap);
 }
 
 __device__ __forceinline__ RowSource row_source(const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                                const sim::DeviceParams& dp, uint32_t sc) {
+                                                const SceneView& v, uint32_t sc) {
     RowSource r;
-    decode_key(key_s[sc], dp.grid.dim, r.cx, r.cy, r.cz);
-    r.reach = neighbour_reach(dp);
-    r.dim = dp.grid.dim;
-    r.lb = lb;
+    decode_key(key_s[sc] - v.cellOffset, v.dp->grid.dim, r.cx, r.cy, r.cz);
+    r.reach = neighbour_reach(*v.dp);
+    r.dim = v.dp->grid.dim;
+    r.lb = lb + v.cellOffset;
     return r;
 }
 
@@ -197,46 +239,83 @@ __device__ __forceinline__ void stage_tile(const TilePlan& P, const float4* __re
     }
 }
 
+// Plans the CTA's tile and stages it when it is staged and its scene has
+// lists; returns whether the tile is staged.  CTA-uniform; every thread
+// calls it.
+template <class Scenes>
+__device__ __forceinline__ bool plan_and_stage(TilePlan& P, const uint32_t* __restrict__ key_s,
+                                               const uint32_t* __restrict__ lb, const Scenes& S,
+                                               const ListBufs& lbuf, uint32_t t0, uint32_t N,
+                                               const float4* __restrict__ pos, const float* __restrict__ lam,
+                                               const float4* __restrict__ vel, float4* sp, float2* sv) {
+    if (lbuf.cap == 0) return false;
+    if (threadIdx.x < 32) plan_tile(P, key_s, lb, S, lbuf, t0, N);
+    __syncthreads();
+    const bool staged = P.staged && P.lists && lbuf.staging;
+    if (staged) stage_tile(P, pos, lam, vel, sp, sv);
+    __syncthreads();
+    return staged;
+}
+
 // Builds the neighbour lists: a warp takes its 32 particles one at a time,
 // 32 candidates per step, and a ballot compacts the candidates within the
 // list radius into the particle's list in walk order (coalesced stores).
 // Entries are 16-bit stage indices in staged tiles, 32-bit sorted slots
-// otherwise; each warp derives its tile's plan itself.
+// otherwise; each warp derives its tile's plan itself.  A particle whose
+// scene has no lists gets the count cap + 1 (its warp walks the stencil).
 constexpr int kBuildBS = 256;
 static_assert(kTile % 32 == 0, "tiles are whole warps");
+template <class Scenes>
 __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restrict__ pred,
                                                           const uint32_t* __restrict__ key_s,
-                                                          const uint32_t* __restrict__ lb,
-                                                          const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                          int updates, uint32_t cap, uint32_t* __restrict__ list,
-                                                          uint32_t* __restrict__ count, uint32_t* __restrict__ stats,
-                                                          int staging) {
-    const sim::DeviceParams& dp = *dpp;
-    float R2;
-    if (!list_radius2(dp, updates, R2)) return;
+                                                          const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
+                                                          ListBufs lbuf, uint32_t* __restrict__ list,
+                                                          uint32_t* __restrict__ count, uint32_t* __restrict__ stats) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t s0 = (blockIdx.x * kBuildBS + threadIdx.x) & ~31u;
     if (s0 >= N) return;  // warp-uniform
-    const WarpPlan plan = plan_tile_warp(key_s, lb, dp, s0 - s0 % uint32_t(kTile), N);
-    const bool staged = plan.staged && staging;
+    const uint32_t cap = lbuf.cap;
+    const WarpPlan plan = plan_tile_warp(key_s, lb, S, lbuf, s0 - s0 % uint32_t(kTile), N);
+    const bool staged = plan.staged && lbuf.staging;
     const uint32_t planShift = plan.base - plan.start;  // lane r: stage index of slot k in row r is k + shift
-    const int reach = neighbour_reach(dp);
-    const int side = 2 * reach + 1;
-    const int nrows = side * side;
-    const int3 dim = dp.grid.dim;
     const uint32_t lt = lanemask_lt();
     uint32_t longest = 0, overflowed = 0;
     const uint32_t pend = min(N - s0, 32u);
     for (uint32_t p = 0; p < pend; ++p) {
         const uint32_t s = s0 + p;
+        const SceneView v = S.view(s);  // warp-uniform: one particle at a time
+        const sim::DeviceParams& dp = *v.dp;
+        float R2;
+        if (v.listUpdates < 0 || !list_radius2(dp, v.listUpdates, R2)) {
+            if (lane == 0) count[s] = cap + 1u;
+            continue;
+        }
+        const int reach = neighbour_reach(dp);
+        const int side = 2 * reach + 1;
+        const int nrows = side * side;
+        const int3 dim = dp.grid.dim;
+        const uint32_t* slb = lb + v.cellOffset;
         const float4 pi = pred[s];
         int cx, cy, cz;
-        decode_key(key_s[s], dim, cx, cy, cz);
+        decode_key(key_s[s] - v.cellOffset, dim, cx, cy, cz);
         const int x0 = max(cx - reach, 0);
         const int x1 = min(cx + reach, dim.x - 1);
         uint32_t* out32 = list + size_t(s) * cap;
         uint16_t* out16 = reinterpret_cast<uint16_t*>(out32);
         uint32_t cnt = 0;
+        // One candidate test per lane and step; `emit` compacts the step's
+        // hits into the list (warp-uniform call).
+        auto emit = [&](bool in, uint32_t k, uint32_t shift) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+            const uint32_t at = cnt + __popc(m & lt);
+            if (in && at < cap) {
+                if (staged)
+                    out16[at] = uint16_t(k + shift);
+                else
+                    out32[at] = k;
+            }
+            cnt += __popc(m);
+        };
         for (int r0 = 0; r0 < nrows; r0 += 32) {
             // this batch's row ranges, one row per lane
             const int r = r0 + int(lane);
@@ -246,11 +325,48 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                 const int y = cy + r % side - reach;
                 if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
                     const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
-                    rb = __ldg(lb + row + uint32_t(x0));
-                    re = __ldg(lb + row + uint32_t(x1) + 1u);
+                    rb = __ldg(slb + row + uint32_t(x0));
+                    re = __ldg(slb + row + uint32_t(x1) + 1u);
                 }
             }
             const int nr = min(32, nrows - r0);
+            if (nrows == 9) {
+                // Short rows (sparse regions): walk the 9 rows as one
+                // flattened sequence, 32 candidates per step whatever the row
+                // lengths, when that takes fewer steps' worth of instructions
+                // than row by row.
+                const uint32_t len = re - rb;
+                uint32_t end = len;  // inclusive prefix: end of row r in the flattened sequence
+#pragma unroll
+                for (int o = 1; o < 16; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, end, o);
+                    if (int(lane) >= o) end += t;
+                }
+                const uint32_t T = __shfl_sync(0xFFFFFFFFu, end, 8);
+                const uint32_t rowSteps = __reduce_add_sync(0xFFFFFFFFu, (len + 31u) >> 5);
+                if (((T + 31u) >> 5) * 2u < rowSteps) {
+                    uint32_t ends[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) ends[q] = __shfl_sync(0xFFFFFFFFu, end, q);
+                    const uint32_t startOf = end - len;
+                    for (uint32_t c = 0; c < T; c += 32u) {
+                        const uint32_t vi = c + lane;
+                        uint32_t row = 0;
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) row += (ends[q] <= vi) ? 1u : 0u;
+                        const uint32_t k = __shfl_sync(0xFFFFFFFFu, rb, int(row)) +
+                                           (vi - __shfl_sync(0xFFFFFFFFu, startOf, int(row)));
+                        const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, int(row));
+                        bool in = false;
+                        if (vi < T) {
+                            float rx, ry, rz;
+                            in = k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > R2);
+                        }
+                        emit(in, k, shift);
+                    }
+                    break;  // nrows == 9: a single batch
+                }
+            }
             for (int rr = 0; rr < nr; ++rr) {
                 const uint32_t b = __shfl_sync(0xFFFFFFFFu, rb, rr);
                 const uint32_t e = __shfl_sync(0xFFFFFFFFu, re, rr);
@@ -264,15 +380,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                         float rx, ry, rz;
                         in = k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > R2);
                     }
-                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
-                    const uint32_t at = cnt + __popc(m & lt);
-                    if (in && at < cap) {
-                        if (staged)
-                            out16[at] = uint16_t(k + shift);
-                        else
-                            out32[at] = k;
-                    }
-                    cnt += __popc(m);
+                    emit(in, k, shift);
                 }
             }
         }
@@ -297,10 +405,11 @@ constexpr size_t kSolveSmem = kStageBytes + size_t(kQueue) * kTile * sizeof(uint
 constexpr size_t kCommitSmem = kStageBytes + size_t(kStageMax) * sizeof(float2);
 static_assert(size_t(kQueue) * kTile * sizeof(uint32_t) <= kStageBytes, "32-bit queues fit in the stage area");
 
-__global__ void __launch_bounds__(kTile) k_lambda(const float4* __restrict__ pred, const uint32_t* __restrict__ key_s,
-                                                  const uint32_t* __restrict__ lb,
-                                                  const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                  float* __restrict__ lam, ListArgs la) {
+// lambda of iteration `it` for every slot whose scene runs that iteration.
+template <class Scenes>
+__global__ void __launch_bounds__(kTile) k_lambda(int it, const float4* __restrict__ pred,
+                                                  const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                                  Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -308,23 +417,17 @@ __global__ void __launch_bounds__(kTile) k_lambda(const float4* __restrict__ pre
     uint32_t* q32 = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
     const uint32_t t0 = blockIdx.x * kTile;
     const uint32_t s = t0 + threadIdx.x;
-    const bool active = s < N;  // every lane takes part in the warp-wide rounds
-    const uint32_t sc = active ? s : 0u;
-    const sim::DeviceParams& dp = *dpp;
-    const bool lists = lists_usable(la, dp);
-    if (lists) {
-        if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
-        __syncthreads();
-        if (P.staged && la.staging) stage_tile(P, pred, nullptr, nullptr, sp, nullptr);
-        __syncthreads();
-    }
-    const bool staged = lists && P.staged && la.staging;
+    const uint32_t sc = s < N ? s : 0u;
+    const SceneView v = S.view(sc);
+    const sim::DeviceParams& dp = *v.dp;
+    const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
+    const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, nullptr, sp, nullptr);
     const float4 pi = pred[sc];
     const GlobalData g{pred, nullptr, nullptr};
     uint32_t n;
     float l = 0.f;
-    if (lists && warp_lists_fit(la, active, sc, n)) {
-        const uint32_t* base = la.list + size_t(sc) * la.cap;
+    if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+        const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             l = lambda_queued<kQueue, kTile>(active, sc, pi,
                                              ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
@@ -333,24 +436,28 @@ __global__ void __launch_bounds__(kTile) k_lambda(const float4* __restrict__ pre
             l = lambda_queued<kQueue, kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
     } else if (staged) {
         int cx, cy, cz;
-        decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+        decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            l = lambda_of(sc, pi, cx, cy, cz, dp, LbRows{lb}, [&](uint32_t k, uint32_t& j) {
+            l = lambda_of(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
                 j = k;
                 return __ldg(pred + k);
             });
     } else {
-        l = lambda_queued<kQueue, kTile>(active, sc, pi, row_source(key_s, lb, dp, sc), dp, g, q32);
+        l = lambda_queued<kQueue, kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
     }
     if (active) lam[s] = l;
 }
 
-template <bool kLast>
-__global__ void __launch_bounds__(kTile) k_delta(const float4* __restrict__ pred, const float* __restrict__ lam,
-                                                 const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                                 const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+// delta of iteration `it`.  The scene's last iteration also applies the
+// post-solve boundary (e = 0) and computes v = (x - p)/dt; a scene past its
+// iterations carries its prediction through, and a scene without iterations
+// gets boundary and velocity in pass 0.
+template <class Scenes>
+__global__ void __launch_bounds__(kTile) k_delta(int it, const float4* __restrict__ pred,
+                                                 const float* __restrict__ lam, const uint32_t* __restrict__ key_s,
+                                                 const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
                                                  float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
-                                                 float4* __restrict__ vel_s, ListArgs la) {
+                                                 float4* __restrict__ vel_s, ListBufs lbuf) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -358,25 +465,19 @@ __global__ void __launch_bounds__(kTile) k_delta(const float4* __restrict__ pred
     uint32_t* q32 = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
     const uint32_t t0 = blockIdx.x * kTile;
     const uint32_t s = t0 + threadIdx.x;
-    const bool active = s < N;  // every lane takes part in the warp-wide rounds
-    const uint32_t sc = active ? s : 0u;
-    const sim::DeviceParams& dp = *dpp;
-    const bool lists = lists_usable(la, dp);
-    if (lists) {
-        if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
-        __syncthreads();
-        if (P.staged && la.staging) stage_tile(P, pred, lam, nullptr, sp, nullptr);
-        __syncthreads();
-    }
-    const bool staged = lists && P.staged && la.staging;
+    const uint32_t sc = s < N ? s : 0u;
+    const SceneView v = S.view(sc);
+    const sim::DeviceParams& dp = *v.dp;
+    const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
+    const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, lam, nullptr, sp, nullptr);
     const float4 pi = pred[sc];
     const float lam_i = lam[sc];
     const float w_q = scorr_wq(dp);
     const GlobalData g{pred, lam, nullptr};
     uint32_t n;
     float3 d = make_float3(0.f, 0.f, 0.f);
-    if (lists && warp_lists_fit(la, active, sc, n)) {
-        const uint32_t* base = la.list + size_t(sc) * la.cap;
+    if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+        const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i,
                                             ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
@@ -386,19 +487,21 @@ __global__ void __launch_bounds__(kTile) k_delta(const float4* __restrict__ pred
                                             q32);
     } else if (staged) {
         int cx, cy, cz;
-        decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
+        decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            d = delta_of(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb}, [&](uint32_t k, uint32_t& j, float& lj) {
-                j = k;
-                lj = __ldg(lam + k);
-                return __ldg(pred + k);
-            });
+            d = delta_of(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb + v.cellOffset},
+                         [&](uint32_t k, uint32_t& j, float& lj) {
+                             j = k;
+                             lj = __ldg(lam + k);
+                             return __ldg(pred + k);
+                         });
     } else {
-        d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i, row_source(key_s, lb, dp, sc), dp, w_q, g, q32);
+        d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
     }
-    if (!active) return;
-    float4 x = make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w);
-    if (kLast) {
+    if (s >= N) return;
+    const bool last = active ? it == v.iters - 1 : (v.iters <= 0 && it == 0);
+    float4 x = active ? make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w) : pi;
+    if (last) {
         // Boundary(e=0) after the solve loop (sim/phases.cpp:94); its velocity
         // half is overwritten by the velocity phase, so only x is clamped.
         float4 vdummy = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -428,64 +531,61 @@ __global__ void __launch_bounds__(kBS) k_finalize_no_iters(float4* __restrict__ 
     pred[s] = x;
 }
 
-template <bool kXsph>
+// XSPH (Jacobi, where the scene configures it), boundary(e), scatter to ids.
+template <class Scenes, bool kXsph>
 __global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                                  const uint32_t* __restrict__ perm,
-                                                  const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                  float4* __restrict__ pos, float4* __restrict__ vel, ListArgs la) {
+                                                  const uint32_t* __restrict__ perm, Scenes S, uint32_t N,
+                                                  float4* __restrict__ pos, float4* __restrict__ vel, ListBufs lbuf) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     const uint32_t t0 = blockIdx.x * kTile;
     const uint32_t s = t0 + threadIdx.x;
-    const bool active = s < N;  // every lane takes part in the warp-wide rounds
-    const uint32_t sc = active ? s : 0u;
-    const sim::DeviceParams& dp = *dpp;
+    const uint32_t sc = s < N ? s : 0u;
+    const SceneView v = S.view(sc);
+    const sim::DeviceParams& dp = *v.dp;
     float4 x = pred[sc];
-    float4 v = vel_s[sc];
-    if (kXsph && dp.xsph_c > 0.f) {
+    float4 vv = vel_s[sc];
+    if (kXsph) {
         float4* sp = smem;
         float2* sv = reinterpret_cast<float2*>(smem + kStageMax);
-        const bool lists = lists_usable(la, dp);
-        if (lists) {
-            if (threadIdx.x < 32) plan_tile(P, key_s, lb, dp, t0, N);
-            __syncthreads();
-            if (P.staged && la.staging) stage_tile(P, pred, nullptr, vel_s, sp, sv);
-            __syncthreads();
-        }
-        const bool staged = lists && P.staged && la.staging;
+        const bool xs = s < N && dp.xsph_c > 0.f;  // every lane takes part in the warp-wide rounds
+        const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, vel_s, sp, sv);
         // Queue of the queued walks: the stage area, free in tiles that are
         // not staged.  In a staged tile a warp whose lists overflowed walks
         // the stencil without a queue.
         uint32_t* q = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
         const GlobalData g{pred, nullptr, vel_s};
         uint32_t n;
-        if (lists && warp_lists_fit(la, active, sc, n)) {
-            const uint32_t* base = la.list + size_t(sc) * la.cap;
+        float4 vx = vv;
+        if (warp_lists_fit(lbuf, xs, scene_lists(v, lbuf), sc, n)) {
+            const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
             if (staged)
-                v = xsph_list_inline(active, x, v,
-                                     ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
-                                     StagedData{sp, sv});
+                vx = xsph_list_inline(xs, x, vv,
+                                      ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                      StagedData{sp, sv});
             else
-                v = xsph_queued<kQueue, kTile>(active, sc, x, v, ListSource<uint32_t>{base, n, sc}, dp, g, q);
+                vx = xsph_queued<kQueue, kTile>(xs, sc, x, vv, ListSource<uint32_t>{base, n, sc}, dp, g, q);
         } else if (staged) {
             int cx, cy, cz;
-            decode_key(key_s[sc], dp.grid.dim, cx, cy, cz);
-            if (active)
-                v = xsph_of(sc, x, v, cx, cy, cz, dp, LbRows{lb}, [&](uint32_t k, uint32_t& j, float4& vj) {
-                    j = k;
-                    vj = __ldg(vel_s + k);
-                    return __ldg(pred + k);
-                });
+            decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
+            if (xs)
+                vx = xsph_of(sc, x, vv, cx, cy, cz, dp, LbRows{lb + v.cellOffset},
+                             [&](uint32_t k, uint32_t& j, float4& vj) {
+                                 j = k;
+                                 vj = __ldg(vel_s + k);
+                                 return __ldg(pred + k);
+                             });
         } else {
-            v = xsph_queued<kQueue, kTile>(active, sc, x, v, row_source(key_s, lb, dp, sc), dp, g, q);
+            vx = xsph_queued<kQueue, kTile>(xs, sc, x, vv, row_source(key_s, lb, v, sc), dp, g, q);
         }
+        if (xs) vv = vx;
     }
-    if (!active) return;
-    boundary_apply(x, v, dp.grid, dp.boundaryRestitution);
+    if (s >= N) return;
+    boundary_apply(x, vv, dp.grid, dp.boundaryRestitution);
     const uint32_t i = perm[s];
     pos[i] = x;
-    vel[i] = v;
+    vel[i] = vv;
 }
 
 __global__ void k_scatter_lambda(const float* __restrict__ lam_s, const uint32_t* __restrict__ perm, uint32_t N,
@@ -648,10 +748,13 @@ int list_updates(const FusedShape& sh, int it) {
     return it >= sh.iters ? -1 : sh.list_span - 1;
 }
 
-ListArgs list_args(const FusedBufs& b, const FusedShape& sh, int it) {
-    ListArgs la{b.nbr_list, b.nbr_count, b.nbr_cap, -1, b.nbr_staging ? 1 : 0};
-    if (lists_on(b, sh)) la.updates = list_updates(sh, it);
-    return la;
+ListBufs list_bufs(const FusedBufs& b, const FusedShape& sh) {
+    if (!lists_on(b, sh)) return ListBufs{nullptr, nullptr, 0u, 0};
+    return ListBufs{b.nbr_list, b.nbr_count, b.nbr_cap, b.nbr_staging ? 1 : 0};
+}
+
+OneScene one_scene(const FusedBufs& b, const FusedShape& sh, int it) {
+    return OneScene{b.dp, sh.iters, lists_on(b, sh) ? list_updates(sh, it) : -1};
 }
 
 }  // namespace
@@ -673,14 +776,14 @@ cudaError_t fused_prepare_kernels() {
     std::lock_guard<std::mutex> lock(mu);
     if (done[dev]) return cudaSuccess;
     const int solve = int(kSolveSmem), commit = int(kCommitSmem);
-    if ((e = cudaFuncSetAttribute(k_lambda, cudaFuncAttributeMaxDynamicSharedMemorySize, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, solve)) !=
-            cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_commit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, commit)) !=
-            cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_commit<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, commit)) !=
-            cudaSuccess)
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if ((e = cudaFuncSetAttribute(k_lambda<OneScene>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_lambda<ManyScenes>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<OneScene>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<ManyScenes>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<OneScene, true>, a, commit)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<OneScene, false>, a, commit)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<ManyScenes, true>, a, commit)) != cudaSuccess)
         return e;
     done[dev] = true;
     return cudaSuccess;
@@ -689,9 +792,9 @@ cudaError_t fused_prepare_kernels() {
 cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, cudaStream_t s) {
     if (sh.N == 0 || !lists_on(b, sh) || it < 0 || it >= sh.iters || it % sh.list_span != 0) return cudaErrorNotReady;
     const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
-    k_build_lists<<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(cur, b.key_s, b.lb, b.dp, sh.N,
-                                                                 list_updates(sh, it), b.nbr_cap, b.nbr_list,
-                                                                 b.nbr_count, b.nbr_stats, b.nbr_staging ? 1 : 0);
+    k_build_lists<<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N,
+                                                                 list_bufs(b, sh), b.nbr_list, b.nbr_count,
+                                                                 b.nbr_stats);
     return cudaGetLastError();
 }
 
@@ -703,16 +806,12 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
     // iteration it reads buffer (it even ? a : b) and writes the other one
     float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
     float4* nxt = (it % 2 == 0) ? b.pred_b : b.pred_a;
-    const ListArgs la = list_args(b, sh, it);
-    if (which == 0) {
-        k_lambda<<<g, kTile, kSolveSmem, s>>>(cur, b.key_s, b.lb, b.dp, sh.N, b.lam_s, la);
-    } else if (it == sh.iters - 1) {
-        k_delta<true><<<g, kTile, kSolveSmem, s>>>(cur, b.lam_s, b.key_s, b.lb, b.dp, sh.N, nxt, b.pos_s, b.vel_s,
-                                                   la);
-    } else {
-        k_delta<false><<<g, kTile, kSolveSmem, s>>>(cur, b.lam_s, b.key_s, b.lb, b.dp, sh.N, nxt, b.pos_s, b.vel_s,
-                                                    la);
-    }
+    const OneScene sc = one_scene(b, sh, it);
+    if (which == 0)
+        k_lambda<<<g, kTile, kSolveSmem, s>>>(it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh));
+    else
+        k_delta<<<g, kTile, kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s,
+                                            list_bufs(b, sh));
     return cudaGetLastError();
 }
 
@@ -735,12 +834,50 @@ cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t 
     if (e != cudaSuccess) return e;
     const float4* x = fused_final_pred(b, sh);
     const unsigned g = blocks_for(sh.N, kTile);
-    const ListArgs la = list_args(b, sh, sh.iters);
+    const OneScene sc = one_scene(b, sh, sh.iters);
+    const ListBufs lb = list_bufs(b, sh);
     if (sh.xsph)
-        k_commit<true><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, b.dp, sh.N, b.pos, b.vel, la);
+        k_commit<OneScene, true><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc, sh.N, b.pos,
+                                                             b.vel, lb);
     else
-        k_commit<false><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, b.dp, sh.N, b.pos, b.vel,
-                                                      la);
+        k_commit<OneScene, false><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc, sh.N, b.pos,
+                                                              b.vel, lb);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ many scenes
+cudaError_t multi_build_lists(const MultiBufs& m, cudaStream_t s) {
+    if (m.N == 0 || m.nbr_cap == 0) return cudaSuccess;
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
+    k_build_lists<<<blocks_for(m.N, kBuildBS), kBuildBS, 0, s>>>(m.pred_a, m.key_s, m.lb,
+                                                                ManyScenes{m.scenes, m.sceneOfSlot}, m.N, lb,
+                                                                m.nbr_list, m.nbr_count, m.nbr_stats);
+    return cudaGetLastError();
+}
+
+cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_t s) {
+    if (m.N == 0) return cudaSuccess;
+    cudaError_t e = fused_prepare_kernels();
+    if (e != cudaSuccess) return e;
+    const unsigned g = blocks_for(m.N, kTile);
+    float4* cur = (it % 2 == 0) ? m.pred_a : m.pred_b;
+    float4* nxt = (it % 2 == 0) ? m.pred_b : m.pred_a;
+    const ManyScenes sc{m.scenes, m.sceneOfSlot};
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
+    if (which == 0)
+        k_lambda<<<g, kTile, kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N, m.lam_s, lb);
+    else
+        k_delta<<<g, kTile, kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N, nxt, m.pos_s, m.vel_s, lb);
+    return cudaGetLastError();
+}
+
+cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStream_t s) {
+    if (m.N == 0) return cudaSuccess;
+    cudaError_t e = fused_prepare_kernels();
+    if (e != cudaSuccess) return e;
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
+    k_commit<ManyScenes, true><<<blocks_for(m.N, kTile), kTile, kCommitSmem, s>>>(
+        final_pred, m.vel_s, m.key_s, m.lb, m.perm, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, m.pos, m.vel, lb);
     return cudaGetLastError();
 }
 

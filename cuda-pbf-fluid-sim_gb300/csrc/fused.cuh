@@ -103,6 +103,38 @@ inline float4* fused_final_pred(const FusedBufs& b, const FusedShape& sh) {
     return (sh.iters % 2 == 0) ? b.pred_a : b.pred_b;
 }
 
+// ------------------------------------------------------------ many scenes
+// One scene of a batch: its parameters, its first cell in the batch's global
+// cell numbering, its solver iterations and the position updates its
+// neighbour lists cover (-1: the scene walks the stencil).
+struct SceneInfo {
+    sim::DeviceParams dp;
+    uint32_t cellOffset;
+    int iters;
+    int listUpdates;
+    int pad;
+};
+
+// Buffers of a batch of scenes (sorted slots over all scenes).
+struct MultiBufs {
+    uint32_t N;
+    const SceneInfo* scenes;
+    const uint32_t* sceneOfSlot;
+    float4 *pos, *vel, *pred_a, *pred_b, *pos_s, *vel_s;
+    float* lam_s;
+    const uint32_t *key_s, *perm, *lb;
+    uint32_t *nbr_list, *nbr_count, *nbr_stats;
+    uint32_t nbr_cap;  // 0: no lists
+};
+
+// The list passes of a batch: lists built once from the prediction (for the
+// scenes whose listUpdates >= 0), lambda / delta of iteration `it` for every
+// scene that runs it (scenes past their iterations carry the prediction
+// through), and XSPH + boundary + scatter.
+cudaError_t multi_build_lists(const MultiBufs& m, cudaStream_t s);
+cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_t s);
+cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStream_t s);
+
 // Density statistics of the committed state (fresh grid; uses pred_b/pos_s
 // as scratch).  Writes 4 doubles to b.stats_out.
 cudaError_t fused_density_stats(const FusedBufs& b, const FusedShape& sh, cudaStream_t s);
