@@ -53,6 +53,16 @@ CONFIGS = {
     "c2_dense": dict(box=(2.0, 1.0, 2.0), lattice=(128, 64, 128), iters=2, hashed=False,
                      workload="dam_break_1M_2iter_dense (128x64x128 lattice, [0,2]x[0,1]x[0,2] box)"),
     # adjoint: 32 scenes of a 64^3 lattice in a 1 m box, 60 steps, checkpoints every 10
+    # 8.4M-particle slab plus a 1M block dropped 0.5 m above it (x, z seeded),
+    # 4 iterations; the box is 2.5 m high so the second block fits
+    "c3": dict(box=(3.0, 2.5, 3.0), lattice=(256, 128, 256), iters=4, hashed=True, drop=(128, 64, 128, 0.5),
+               list_capacity=1024, metric="particle-steps/s @9.4M",
+               workload="dam_break_9.4M_4iter_hashed (256x128x256 lattice + 128x64x128 block 0.5 m above, "
+                        "[0,3]x[0,2.5]x[0,3] box)"),
+    "c3_dense": dict(box=(3.0, 2.5, 3.0), lattice=(256, 128, 256), iters=4, hashed=False, drop=(128, 64, 128, 0.5),
+                     list_capacity=1024, metric="particle-steps/s @9.4M",
+                     workload="dam_break_9.4M_4iter_dense (256x128x256 lattice + 128x64x128 block 0.5 m above, "
+                              "[0,3]x[0,2.5]x[0,3] box)"),
     # (65,536 particles per scene: a 64x32x32 lattice; a 64^3 one would hold 262,144)
     "c5": dict(adjoint=True, scenes=32, lattice=(64, 32, 32), box=(1.0, 1.0, 1.0), iters=2, hashed=True,
                horizon=60, every=10, res=32,
@@ -209,6 +219,18 @@ def scene(lib, cfg):
     n = nx * ny * nz
     p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
     pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
+    if "drop" in cfg:
+        # a second block, its bottom `gap` above the first block's top, at a
+        # seeded (x, z) inside the box
+        bx, by, bz, gap = cfg["drop"]
+        rng = np.random.default_rng(0xD209)
+        ox = 0.005 + rng.uniform(0.0, cfg["box"][0] - 0.01 * bx - 0.01)
+        oz = 0.005 + rng.uniform(0.0, cfg["box"][2] - 0.01 * bz - 0.01)
+        oy = 0.005 + 0.01 * ny + gap
+        q = pbfx.dam_break_params(cfg["box"], cfg["iters"], n + bx * by * bz)
+        pos2 = pbfx.seed_lattice(lib, bx, by, bz, (ox, oy, oz), 0.01, 0.0005, 0xC0FFEE + 1, q)
+        pos = np.ascontiguousarray(np.concatenate([pos, pos2]))
+        p = q
     return p, pos, np.zeros_like(pos)
 
 
@@ -247,7 +269,8 @@ def run_reference(args, cfg, world, rank):
     sample = ("%d of the %d requested steps of the %d-particle workload after %d warm-up steps "
               "(time budget %.0f s)" % (steps, args.steps, n, args.warmup, args.ref_budget))
     line = {
-        "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": steps,
+        "metric": cfg.get("metric", METRIC), "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": world,
+        "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
         "config": {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"],
@@ -280,6 +303,8 @@ def run_ours(args, cfg, world, rank, local):
     hbm_peak, peak_kind = peaks()
 
     sim = pbfx.Sim(lib, p, hashed=hashed)
+    if "list_capacity" in cfg:
+        sim.set_list_capacity(cfg["list_capacity"])
     sim.upload(pos, vel)
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -352,7 +377,8 @@ def run_ours(args, cfg, world, rank, local):
     sim.close()
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "metric": cfg.get("metric", METRIC), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup,
         "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded jittered lattice, mt19937_64 0xC0FFEE)",
         "config": {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"], "cells": nc,
