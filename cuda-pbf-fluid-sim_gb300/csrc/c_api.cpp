@@ -534,6 +534,29 @@ int pbf_debug_eval_math(int fn, const float* a, const float* b, float* out, uint
     return from_cuda(cudaDeviceSynchronize());
 }
 
+int pbf_selftest_powf4(uint64_t* mismatches, uint32_t* first_mismatch_bits) {
+    if (!mismatches) return PBF_ERR_INVALID;
+    unsigned long long* dm = nullptr;
+    uint32_t* df = nullptr;
+    if (cudaMalloc(&dm, sizeof(*dm)) != cudaSuccess || cudaMalloc(&df, sizeof(*df)) != cudaSuccess) {
+        cudaFree(dm);
+        return PBF_ERR_OOM;
+    }
+    // n passes through a volatile host variable so the kernel sees it only at run time
+    volatile float four = 4.0f;
+    cudaError_t e = pbf::selftest_powf4(four, dm, df, 0);
+    unsigned long long hm = 0;
+    uint32_t hf = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&hm, dm, sizeof(hm), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&hf, df, sizeof(hf), cudaMemcpyDeviceToHost);
+    cudaFree(dm);
+    cudaFree(df);
+    if (e != cudaSuccess) return from_cuda(e);
+    *mismatches = hm;
+    if (first_mismatch_bits) *first_mismatch_bits = hf;
+    return PBF_OK;
+}
+
 int pbf_selftest_bounded_wait(uint32_t spin_limit, void* d_scratch) {
     if (!d_scratch) return PBF_ERR_INVALID;
     uint32_t* w = static_cast<uint32_t*>(d_scratch);

@@ -178,7 +178,33 @@ __global__ void k_eval_math(int fn, const float* __restrict__ a, const float* __
     out[i] = r;
 }
 
+// scorr_pow(x, 4) against powf(x, n) with n = 4 known only at run time, on
+// every non-negative float bit pattern up to +inf, 16 per thread.
+__global__ void k_selftest_powf4(float n, unsigned long long* __restrict__ mismatches, uint32_t* __restrict__ first) {
+    const uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * 16u;
+    unsigned long long local = 0;
+    for (uint32_t u = 0; u < 16u; ++u) {
+        const uint32_t bits = base + u;
+        if (bits > 0x7F800000u) break;
+        const float x = __uint_as_float(bits);
+        if (__float_as_uint(scorr_pow(x, 4.0f)) != __float_as_uint(powf(x, n))) {
+            ++local;
+            atomicMin(first, bits);
+        }
+    }
+    if (local) atomicAdd(mismatches, local);
+}
+
 }  // namespace
+
+cudaError_t selftest_powf4(float n_runtime, unsigned long long* d_mismatches, uint32_t* d_first, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(d_mismatches, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_first, 0xFF, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const uint32_t threads = 0x7F800000u / 16u + 1u;
+    k_selftest_powf4<<<blocks_for(threads, 256), 256, 0, s>>>(n_runtime, d_mismatches, d_first);
+    return cudaGetLastError();
+}
 
 cudaError_t eval_math(int fn, const float* a, const float* b, float* out, uint32_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;

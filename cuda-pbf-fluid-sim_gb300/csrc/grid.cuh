@@ -38,6 +38,10 @@ cudaError_t launch_compact(void* d_scratch, size_t scratch_bytes, uint32_t* uniq
 // Device powf (fn 0), sqrtf (fn 1), division (fn 2) on arrays.
 cudaError_t eval_math(int fn, const float* a, const float* b, float* out, uint32_t n, cudaStream_t s);
 
+// Exhaustive check of the s_corr exponent's n = 4 form (see
+// pbf_selftest_powf4); n_runtime must be 4.
+cudaError_t selftest_powf4(float n_runtime, unsigned long long* d_mismatches, uint32_t* d_first, cudaStream_t s);
+
 // Bounded-wait self-test (see pbf_selftest_bounded_wait).
 cudaError_t selftest_bounded_wait(uint32_t spin_limit, uint32_t* d_scratch4, cudaStream_t s);
 

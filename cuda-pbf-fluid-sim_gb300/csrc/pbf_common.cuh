@@ -524,7 +524,13 @@ __device__ __forceinline__ float lambda_queued(bool active, uint32_t s, float4 p
 }
 
 // s_corr exponent: powf, as the reference (sim/pbf_delta_apply.cu:82).
-__device__ __forceinline__ float scorr_pow(float ratio, float n) { return powf(ratio, n); }
+// With n = 4 exactly (the reference's default) the call names the exponent
+// at compile time, which the compiler evaluates with ~19 fewer instructions;
+// both forms return the same float for every non-negative input
+// (pbf_selftest_powf4 compares them over all 2^31 non-negative bit patterns).
+__device__ __forceinline__ float scorr_pow(float ratio, float n) {
+    return (n == 4.0f) ? powf(ratio, 4.0f) : powf(ratio, n);
+}
 
 // w_q of the tensile-instability term (sim/pbf_delta_apply.cu:40-42).
 __device__ __forceinline__ float scorr_wq(const sim::DeviceParams& dp) {

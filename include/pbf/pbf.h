@@ -329,6 +329,15 @@ int pbf_density_grid_loss(pbf_sim* sim, int res, const float* d_target, double* 
  * device arrays: fn 0 = powf(a, b), 1 = sqrtf(a), 2 = a / b (IEEE). */
 int pbf_debug_eval_math(int fn, const float* d_a, const float* d_b, float* d_out, uint32_t n);
 
+/* The delta kernels evaluate s_corr's (w / w_q)^n with the exponent written
+ * as the constant 4 when n == 4, a form the compiler evaluates faster.  This
+ * compares it with powf(x, n) for n = 4 known only at run time on every
+ * non-negative float bit pattern (about 2.1e9 values): *mismatches must be 0
+ * for the results to stay those of the reference kernels.
+ * *first_mismatch_bits (may be NULL) = the smallest mismatching bit pattern,
+ * 0xFFFFFFFF if none. */
+int pbf_selftest_powf4(uint64_t* mismatches, uint32_t* first_mismatch_bits);
+
 /* Failure-path self-test of the bounded device waits: one block polls a
  * look-back status that nothing ever publishes.  After spin_limit polls the
  * kernel records the timeout in its error word and returns, leaving the

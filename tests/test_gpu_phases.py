@@ -310,3 +310,13 @@ def test_bounded_wait_gives_up_and_context_survives(gpu, lib):
     # the context is still usable
     x = torch.arange(10, device="cuda").sum().item()
     assert x == 45
+
+
+def test_scorr_exponent_four_matches_runtime_powf_everywhere(gpu, lib):
+    """The delta kernels' s_corr exponent n == 4 form equals powf(x, n) with n
+    known only at run time, for every non-negative float (2.1e9 values)."""
+    import ctypes as C
+
+    mism, first = C.c_uint64(), C.c_uint32()
+    pbfx.check(lib.pbf_selftest_powf4(C.byref(mism), C.byref(first)), "selftest_powf4")
+    assert mism.value == 0, "first mismatch at bits 0x%08x" % first.value
