@@ -136,6 +136,7 @@ struct pbf_ensemble {
         m.nbr_count = nbrCount;
         m.nbr_stats = nbrStats;
         m.nbr_cap = nbrCap;
+        m.err = err;
         return m;
     }
 
@@ -321,7 +322,8 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
     if (cudaMemcpy(&err, e->err, sizeof(err), cudaMemcpyDeviceToHost) != cudaSuccess) return PBF_ERR_CUDA;
     if (err) {
         cudaMemset(e->err, 0, sizeof(uint32_t));
-        return (err & pbf::kErrLookbackTimeoutBit) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
+        if (err & pbf::kErrLookbackTimeoutBit) return PBF_ERR_TIMEOUT;
+        return (err & pbf::kErrNonFiniteBit) ? PBF_ERR_NONFINITE : PBF_ERR_CUDA;
     }
     return PBF_OK;
 }

@@ -536,7 +536,8 @@ template <class Scenes, bool kXsph>
 __global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   const uint32_t* __restrict__ perm, Scenes S, uint32_t N,
-                                                  float4* __restrict__ pos, float4* __restrict__ vel, ListBufs lbuf) {
+                                                  float4* __restrict__ pos, float4* __restrict__ vel, ListBufs lbuf,
+                                                  uint32_t* __restrict__ err) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     const uint32_t t0 = blockIdx.x * kTile;
@@ -581,8 +582,12 @@ __global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pre
         }
         if (xs) vv = vx;
     }
+    if (s < N) boundary_apply(x, vv, dp.grid, dp.boundaryRestitution);
+    // a NaN / Inf in the committed state is reported through the error word
+    const bool bad = s < N && !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(vv.x) &&
+                                isfinite(vv.y) && isfinite(vv.z));
+    if (__any_sync(0xFFFFFFFFu, bad) && (threadIdx.x & 31u) == 0 && err) atomicOr(err, kErrNonFiniteBit);
     if (s >= N) return;
-    boundary_apply(x, vv, dp.grid, dp.boundaryRestitution);
     const uint32_t i = perm[s];
     pos[i] = x;
     vel[i] = vv;
@@ -838,10 +843,10 @@ cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t 
     const ListBufs lb = list_bufs(b, sh);
     if (sh.xsph)
         k_commit<OneScene, true><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc, sh.N, b.pos,
-                                                             b.vel, lb);
+                                                             b.vel, lb, b.err);
     else
         k_commit<OneScene, false><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc, sh.N, b.pos,
-                                                              b.vel, lb);
+                                                              b.vel, lb, b.err);
     return cudaGetLastError();
 }
 
@@ -877,7 +882,8 @@ cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStrea
     if (e != cudaSuccess) return e;
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     k_commit<ManyScenes, true><<<blocks_for(m.N, kTile), kTile, kCommitSmem, s>>>(
-        final_pred, m.vel_s, m.key_s, m.lb, m.perm, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, m.pos, m.vel, lb);
+        final_pred, m.vel_s, m.key_s, m.lb, m.perm, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, m.pos, m.vel, lb,
+        m.err);
     return cudaGetLastError();
 }
 

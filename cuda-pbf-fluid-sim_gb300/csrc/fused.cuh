@@ -125,6 +125,7 @@ struct MultiBufs {
     const uint32_t *key_s, *perm, *lb;
     uint32_t *nbr_list, *nbr_count, *nbr_stats;
     uint32_t nbr_cap;  // 0: no lists
+    uint32_t* err;     // device error word (kErr* bits)
 };
 
 // The list passes of a batch: lists built once from the prediction (for the

@@ -231,8 +231,10 @@ int pbf_profile_step(pbf_sim* sim, const pbf_sim_params* p, float* ms, const cha
 /* Kernel launches of this library in one pbf_step (graph nodes that are
  * kernels of libpbf_gb300; memsets excluded). */
 int pbf_launches_per_step(pbf_sim* sim);
-/* Wait for the stream and report any device-side error flag
- * (PBF_ERR_TIMEOUT when a bounded wait gave up). */
+/* Wait for the stream and report any device-side error flag:
+ * PBF_ERR_TIMEOUT when a bounded wait gave up, PBF_ERR_NONFINITE when a step
+ * committed a NaN or Inf position or velocity (the state is kept as
+ * computed).  The flags clear once reported. */
 int pbf_synchronize(pbf_sim* sim);
 
 /* Neighbour lists.  No counterpart in the reference, whose solver passes

@@ -182,3 +182,21 @@ def test_step_host_matches_device_path(gpu, lib):
     with pbfx.Sim(lib, p, hashed=True) as s:
         pbfx.check(lib.pbf_step_host(s.h, None, pbfx.ptr(hp), pbfx.ptr(hv)))
     assert np.array_equal(a[0], hp) and np.array_equal(a[1], hv)
+
+
+@pytest.mark.parametrize("hashed", [True, False])
+def test_nonfinite_state_is_reported(gpu, lib, hashed):
+    """A NaN in the state is reported as PBF_ERR_NONFINITE by pbf_synchronize
+    (cell keys clamp it into the grid; nothing faults), the flag clears once
+    reported, and a clean state steps without error again."""
+    p, pos, vel = c1_scene(lib)
+    bad = pos.copy()
+    bad[1234, 1] = np.nan
+    with pbfx.Sim(lib, p, hashed=hashed) as s:
+        s.upload(bad, vel)
+        assert lib.pbf_step_n(s.h, None, 1) == pbfx.PBF_OK
+        assert lib.pbf_synchronize(s.h) == pbfx.PBF_ERR_NONFINITE
+        assert lib.pbf_synchronize(s.h) == pbfx.PBF_OK
+        s.upload(pos, vel)
+        assert lib.pbf_step_n(s.h, None, 2) == pbfx.PBF_OK
+        assert lib.pbf_synchronize(s.h) == pbfx.PBF_OK
