@@ -257,12 +257,64 @@ __device__ __forceinline__ bool plan_and_stage(TilePlan& P, const uint32_t* __re
     return staged;
 }
 
-// Builds the neighbour lists: a warp takes its 32 particles one at a time,
-// 32 candidates per step, and a ballot compacts the candidates within the
-// list radius into the particle's list in walk order (coalesced stores).
-// Entries are 16-bit stage indices in staged tiles, 32-bit sorted slots
-// otherwise; each warp derives its tile's plan itself.  A particle whose
-// scene has no lists gets the count cap + 1 (its warp walks the stencil).
+// Packed two-lane FP32 arithmetic (Blackwell f32x2): the list test of two
+// particles against one candidate in half the instructions.  Each half is an
+// ordinary round-to-nearest FP32 operation.
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(unsigned long long v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// One particle's list being written by a warp: hits of a 32-candidate step
+// are compacted with a ballot into consecutive entries (coalesced stores).
+struct ListWriter {
+    uint32_t* out32;
+    uint16_t* out16;
+    uint32_t cnt;
+    __device__ __forceinline__ void emit(bool in, uint32_t k, uint32_t shift, uint32_t cap, bool staged,
+                                         uint32_t lt) {
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+        const uint32_t at = cnt + __popc(m & lt);
+        if (in && at < cap) {
+            if (staged)
+                out16[at] = uint16_t(k + shift);
+            else
+                out32[at] = k;
+        }
+        cnt += __popc(m);
+    }
+};
+
+// Builds the neighbour lists: a warp takes its 32 particles one at a time
+// (two at a time when consecutive particles share a cell, testing both
+// against each candidate with packed arithmetic), 32 candidates per step,
+// and a ballot compacts the candidates within the list radius into the
+// particle's list in walk order (coalesced stores).  Entries are 16-bit
+// stage indices in staged tiles, 32-bit sorted slots otherwise; each warp
+// derives its tile's plan itself.  The stencil's row ranges are reused while
+// consecutive particles share a cell.  A particle whose scene has no lists
+// gets the count cap + 1 (its warp walks the stencil).
 constexpr int kBuildBS = 256;
 static_assert(kTile % 32 == 0, "tiles are whole warps");
 template <class Scenes>
@@ -281,55 +333,44 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     const uint32_t lt = lanemask_lt();
     uint32_t longest = 0, overflowed = 0;
     const uint32_t pend = min(N - s0, 32u);
-    for (uint32_t p = 0; p < pend; ++p) {
+    // rows of the cell last set up: lane r < nrows holds row r's range
+    uint32_t cachedKey = 0xFFFFFFFFu, rb = 0, re = 0;
+    int nrows = 0;
+    bool flat = false;
+    uint32_t T = 0, startOf = 0, ends[8];
+    float R2 = 0.f;
+    for (uint32_t p = 0; p < pend;) {
         const uint32_t s = s0 + p;
-        const SceneView v = S.view(s);  // warp-uniform: one particle at a time
+        const uint32_t key = key_s[s];
+        const SceneView v = S.view(s);  // warp-uniform: one cell at a time
         const sim::DeviceParams& dp = *v.dp;
-        float R2;
-        if (v.listUpdates < 0 || !list_radius2(dp, v.listUpdates, R2)) {
-            if (lane == 0) count[s] = cap + 1u;
-            continue;
-        }
-        const int reach = neighbour_reach(dp);
-        const int side = 2 * reach + 1;
-        const int nrows = side * side;
-        const int3 dim = dp.grid.dim;
-        const uint32_t* slb = lb + v.cellOffset;
-        const float4 pi = pred[s];
-        int cx, cy, cz;
-        decode_key(key_s[s] - v.cellOffset, dim, cx, cy, cz);
-        const int x0 = max(cx - reach, 0);
-        const int x1 = min(cx + reach, dim.x - 1);
-        uint32_t* out32 = list + size_t(s) * cap;
-        uint16_t* out16 = reinterpret_cast<uint16_t*>(out32);
-        uint32_t cnt = 0;
-        // One candidate test per lane and step; `emit` compacts the step's
-        // hits into the list (warp-uniform call).
-        auto emit = [&](bool in, uint32_t k, uint32_t shift) {
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
-            const uint32_t at = cnt + __popc(m & lt);
-            if (in && at < cap) {
-                if (staged)
-                    out16[at] = uint16_t(k + shift);
-                else
-                    out32[at] = k;
+        if (key != cachedKey) {
+            if (v.listUpdates < 0 || !list_radius2(dp, v.listUpdates, R2)) {
+                if (lane == 0) count[s] = cap + 1u;
+                ++p;
+                continue;
             }
-            cnt += __popc(m);
-        };
-        for (int r0 = 0; r0 < nrows; r0 += 32) {
-            // this batch's row ranges, one row per lane
-            const int r = r0 + int(lane);
-            uint32_t rb = 0, re = 0;
+            const int reach = neighbour_reach(dp);
+            const int side = 2 * reach + 1;
+            nrows = side * side;
+            const int3 dim = dp.grid.dim;
+            int cx, cy, cz;
+            decode_key(key - v.cellOffset, dim, cx, cy, cz);
+            const int x0 = max(cx - reach, 0);
+            const int x1 = min(cx + reach, dim.x - 1);
+            // rows beyond 32 (reach > 2) are set up per batch below
+            rb = re = 0;
+            const int r = int(lane);
             if (r < nrows) {
                 const int z = cz + r / side - reach;
                 const int y = cy + r % side - reach;
                 if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
                     const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
-                    rb = __ldg(slb + row + uint32_t(x0));
-                    re = __ldg(slb + row + uint32_t(x1) + 1u);
+                    rb = __ldg(lb + v.cellOffset + row + uint32_t(x0));
+                    re = __ldg(lb + v.cellOffset + row + uint32_t(x1) + 1u);
                 }
             }
-            const int nr = min(32, nrows - r0);
+            flat = false;
             if (nrows == 9) {
                 // Short rows (sparse regions): walk the 9 rows as one
                 // flattened sequence, 32 candidates per step whatever the row
@@ -342,51 +383,103 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                     const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, end, o);
                     if (int(lane) >= o) end += t;
                 }
-                const uint32_t T = __shfl_sync(0xFFFFFFFFu, end, 8);
+                T = __shfl_sync(0xFFFFFFFFu, end, 8);
                 const uint32_t rowSteps = __reduce_add_sync(0xFFFFFFFFu, (len + 31u) >> 5);
-                if (((T + 31u) >> 5) * 2u < rowSteps) {
-                    uint32_t ends[8];
+                flat = ((T + 31u) >> 5) * 2u < rowSteps;
+                if (flat) {
 #pragma unroll
                     for (int q = 0; q < 8; ++q) ends[q] = __shfl_sync(0xFFFFFFFFu, end, q);
-                    const uint32_t startOf = end - len;
-                    for (uint32_t c = 0; c < T; c += 32u) {
-                        const uint32_t vi = c + lane;
-                        uint32_t row = 0;
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) row += (ends[q] <= vi) ? 1u : 0u;
-                        const uint32_t k = __shfl_sync(0xFFFFFFFFu, rb, int(row)) +
-                                           (vi - __shfl_sync(0xFFFFFFFFu, startOf, int(row)));
-                        const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, int(row));
-                        bool in = false;
-                        if (vi < T) {
-                            float rx, ry, rz;
-                            in = k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > R2);
-                        }
-                        emit(in, k, shift);
-                    }
-                    break;  // nrows == 9: a single batch
+                    startOf = end - len;
                 }
             }
-            for (int rr = 0; rr < nr; ++rr) {
+            cachedKey = key;
+        }
+        // a second particle of the same cell goes along (the row walk only)
+        const bool pair = !flat && nrows <= 32 && p + 1 < pend && key_s[s + 1] == key;
+        const uint32_t sB = pair ? s + 1 : s;
+        const float4 pa = pred[s], pb = pred[sB];
+        ListWriter wa{list + size_t(s) * cap, reinterpret_cast<uint16_t*>(list + size_t(s) * cap), 0u};
+        ListWriter wb{list + size_t(sB) * cap, reinterpret_cast<uint16_t*>(list + size_t(sB) * cap), 0u};
+        if (flat) {
+            for (uint32_t c = 0; c < T; c += 32u) {
+                const uint32_t vi = c + lane;
+                uint32_t row = 0;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) row += (ends[q] <= vi) ? 1u : 0u;
+                const uint32_t k = __shfl_sync(0xFFFFFFFFu, rb, int(row)) +
+                                   (vi - __shfl_sync(0xFFFFFFFFu, startOf, int(row)));
+                const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, int(row));
+                bool in = false;
+                if (vi < T) {
+                    float rx, ry, rz;
+                    in = k != s && !(dist2(pa, __ldg(pred + k), rx, ry, rz) > R2);
+                }
+                wa.emit(in, k, shift, cap, staged, lt);
+            }
+        } else if (nrows <= 32) {
+            const unsigned long long px = pk2(pa.x, pb.x), py = pk2(pa.y, pb.y), pz = pk2(pa.z, pb.z);
+            for (int rr = 0; rr < nrows; ++rr) {
                 const uint32_t b = __shfl_sync(0xFFFFFFFFu, rb, rr);
                 const uint32_t e = __shfl_sync(0xFFFFFFFFu, re, rr);
-                // staged tiles have nrows <= 32, so r0 == 0 and the plan's lane rr is row rr
+                // staged tiles have nrows <= 32, so the plan's lane rr is row rr
                 const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, rr);
 #pragma unroll 2
                 for (uint32_t c = b; c < e; c += 32u) {
                     const uint32_t k = c + lane;
-                    bool in = false;
-                    if (k < e) {
-                        float rx, ry, rz;
-                        in = k != s && !(dist2(pi, __ldg(pred + k), rx, ry, rz) > R2);
+                    const bool valid = k < e;
+                    const float4 pj = valid ? __ldg(pred + k) : pa;
+                    // r^2 = rz^2 + (rx^2 + ry^2), as the neighbour passes compute it
+                    const unsigned long long dx = sub2(px, pk2(pj.x, pj.x)), dy = sub2(py, pk2(pj.y, pj.y)),
+                                             dz = sub2(pz, pk2(pj.z, pj.z));
+                    const float2 r2 = upk2(fma2(dz, dz, fma2(dx, dx, mul2(dy, dy))));
+                    wa.emit(valid && k != s && !(r2.x > R2), k, shift, cap, staged, lt);
+                    if (pair) wb.emit(valid && k != sB && !(r2.y > R2), k, shift, cap, staged, lt);
+                }
+            }
+        } else {
+            // reach > 2: rows in batches of 32, one particle at a time
+            const int reach = neighbour_reach(dp);
+            const int side = 2 * reach + 1;
+            const int3 dim = dp.grid.dim;
+            int cx, cy, cz;
+            decode_key(key - v.cellOffset, dim, cx, cy, cz);
+            const int x0 = max(cx - reach, 0);
+            const int x1 = min(cx + reach, dim.x - 1);
+            for (int r0 = 0; r0 < nrows; r0 += 32) {
+                const int r = r0 + int(lane);
+                uint32_t bb = 0, ee = 0;
+                if (r < nrows) {
+                    const int z = cz + r / side - reach;
+                    const int y = cy + r % side - reach;
+                    if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
+                        const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
+                        bb = __ldg(lb + v.cellOffset + row + uint32_t(x0));
+                        ee = __ldg(lb + v.cellOffset + row + uint32_t(x1) + 1u);
                     }
-                    emit(in, k, shift);
+                }
+                const int nr = min(32, nrows - r0);
+                for (int rr = 0; rr < nr; ++rr) {
+                    const uint32_t b = __shfl_sync(0xFFFFFFFFu, bb, rr);
+                    const uint32_t e = __shfl_sync(0xFFFFFFFFu, ee, rr);
+                    for (uint32_t c = b; c < e; c += 32u) {
+                        const uint32_t k = c + lane;
+                        bool in = false;
+                        if (k < e) {
+                            float rx, ry, rz;
+                            in = k != s && !(dist2(pa, __ldg(pred + k), rx, ry, rz) > R2);
+                        }
+                        wa.emit(in, k, 0u, cap, false, lt);  // nrows > 32: never staged
+                    }
                 }
             }
         }
-        if (lane == 0) count[s] = cnt;
-        longest = max(longest, cnt);
-        overflowed += cnt > cap ? 1u : 0u;
+        if (lane == 0) {
+            count[s] = wa.cnt;
+            if (pair) count[sB] = wb.cnt;
+        }
+        longest = max(longest, pair ? max(wa.cnt, wb.cnt) : wa.cnt);
+        overflowed += (wa.cnt > cap ? 1u : 0u) + (pair && wb.cnt > cap ? 1u : 0u);
+        p += pair ? 2u : 1u;
     }
     if (lane == 0 && stats) {
         atomicMax(stats, longest);

@@ -541,8 +541,9 @@ __device__ __forceinline__ float scorr_wq(const sim::DeviceParams& dp) {
 
 // ----------------------------------------------------------------- delta
 // Position correction, sim/pbf_delta_apply.cu:40-112.
-__device__ __forceinline__ void delta_accumulate(float3& d, float rx, float ry, float rz, float r2, float lam_i,
-                                                 float lam_j, float w_q, const sim::DeviceParams& dp) {
+// One neighbour's term (l_ij, a_ij): the sum is d += l_ij * a_ij per axis.
+__device__ __forceinline__ float4 delta_term(float rx, float ry, float rz, float r2, float lam_i, float lam_j,
+                                             float w_q, const sim::DeviceParams& dp) {
     const sim::KernelCoeffs& kc = dp.kernel;
     const sim::PbfTuning& pbf = dp.pbf;
     const float r = sqrt_(r2);
@@ -558,10 +559,18 @@ __device__ __forceinline__ void delta_accumulate(float3& d, float rx, float ry, 
         scorr = mul_(-pbf.scorr_k, scorr_pow(ratio, pbf.scorr_n));
         if (pbf.scorr_min < 0.f) scorr = fmaxf(scorr, pbf.scorr_min);
     }
-    const float lij = add_(add_(lam_i, lam_j), scorr);
-    d.x = fma_(lij, ax, d.x);
-    d.y = fma_(lij, ay, d.y);
-    d.z = fma_(lij, az, d.z);
+    return make_float4(add_(add_(lam_i, lam_j), scorr), ax, ay, az);
+}
+
+__device__ __forceinline__ void delta_apply_term(float3& d, float4 term) {
+    d.x = fma_(term.x, term.y, d.x);
+    d.y = fma_(term.x, term.z, d.y);
+    d.z = fma_(term.x, term.w, d.z);
+}
+
+__device__ __forceinline__ void delta_accumulate(float3& d, float rx, float ry, float rz, float r2, float lam_i,
+                                                 float lam_j, float w_q, const sim::DeviceParams& dp) {
+    delta_apply_term(d, delta_term(rx, ry, rz, r2, lam_i, lam_j, w_q, dp));
 }
 
 __device__ __forceinline__ float3 delta_finalize(float3 dsum, const sim::DeviceParams& dp) {
