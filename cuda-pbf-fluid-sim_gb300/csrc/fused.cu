@@ -500,7 +500,7 @@ static_assert(size_t(kQueue) * kTile * sizeof(uint32_t) <= kStageBytes, "32-bit 
 
 // lambda of iteration `it` for every slot whose scene runs that iteration.
 template <class Scenes>
-__global__ void __launch_bounds__(kTile) k_lambda(int it, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(kTile, 6) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf) {
     extern __shared__ float4 smem[];
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(kTile) k_lambda(int it, const float4* __restri
     const uint32_t s = t0 + threadIdx.x;
     const uint32_t sc = s < N ? s : 0u;
     const SceneView v = S.view(sc);
-    const sim::DeviceParams& dp = *v.dp;
+    const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
     const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, nullptr, sp, nullptr);
     const float4 pi = pred[sc];
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(kTile) k_lambda(int it, const float4* __restri
 // iterations carries its prediction through, and a scene without iterations
 // gets boundary and velocity in pass 0.
 template <class Scenes>
-__global__ void __launch_bounds__(kTile) k_delta(int it, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(kTile, 6) k_delta(int it, const float4* __restrict__ pred,
                                                  const float* __restrict__ lam, const uint32_t* __restrict__ key_s,
                                                  const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
                                                  float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(kTile) k_delta(int it, const float4* __restric
     const uint32_t s = t0 + threadIdx.x;
     const uint32_t sc = s < N ? s : 0u;
     const SceneView v = S.view(sc);
-    const sim::DeviceParams& dp = *v.dp;
+    const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
     const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, lam, nullptr, sp, nullptr);
     const float4 pi = pred[sc];
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(kBS) k_finalize_no_iters(float4* __restrict__ 
 
 // XSPH (Jacobi, where the scene configures it), boundary(e), scatter to ids.
 template <class Scenes, bool kXsph>
-__global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
+__global__ void __launch_bounds__(kTile, 6) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   const uint32_t* __restrict__ perm, Scenes S, uint32_t N,
                                                   float4* __restrict__ pos, float4* __restrict__ vel, ListBufs lbuf,
@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(kTile) k_commit(const float4* __restrict__ pre
     const uint32_t s = t0 + threadIdx.x;
     const uint32_t sc = s < N ? s : 0u;
     const SceneView v = S.view(sc);
-    const sim::DeviceParams& dp = *v.dp;
+    const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     float4 x = pred[sc];
     float4 vv = vel_s[sc];
     if (kXsph) {

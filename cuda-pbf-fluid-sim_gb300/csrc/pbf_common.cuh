@@ -303,20 +303,24 @@ struct ListSource {
     uint32_t fill;
 };
 
-// Lockstep walk over a neighbour list with the same queueing and draining as
-// walk_queued, over a flat candidate sequence.
+// Lockstep walk over a neighbour list.  Each lane keeps its accepted
+// candidates in a ring of Q entries, first in first out, so every particle
+// still sums its neighbours in list order.  A lane walks its next chunk of
+// eight entries while its ring has room for the chunk; after each round the
+// warp runs as many bodies as every lane with work left has queued (all those
+// lanes busy), and once no list is being walked it empties the rings.
 template <int Q, int kStride, class E, class QT, class Hit, class Body>
 __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E>& src, QT* q, int maxHits,
                                                  Hit&& hit, Body&& body) {
     constexpr int kChunk = 8;
-    static_assert(Q > kChunk, "queue must hold more than one chunk");
-    int cnt = 0, total = 0;
+    static_assert(Q > kChunk && (Q & (Q - 1)) == 0, "the ring holds more than one chunk, a power of two");
+    uint32_t head = 0, cnt = 0;
+    int total = 0;
     uint32_t e = 0;
     const uint32_t n = src.n;
     bool done = !active || n == 0;
     for (;;) {
-        const bool any = __any_sync(0xFFFFFFFFu, !done);
-        if (!done) {
+        if (!done && cnt <= uint32_t(Q - kChunk)) {
             uint32_t ks[kChunk];
             load8(src.lst + e, ks);
 #pragma unroll
@@ -324,19 +328,26 @@ __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E
                 const bool v = !done && e + uint32_t(u) < n;
                 const uint32_t k = v ? ks[u] : src.fill;
                 const bool h = v && hit(k);
-                q[cnt * kStride] = QT(k);  // cnt <= Q - 1 here: at most Q - kChunk queued at a chunk's start
-                cnt += h ? 1 : 0;
+                // cnt + u < Q: the slot is free (live entries are head .. head + cnt - 1)
+                q[((head + cnt) & uint32_t(Q - 1)) * kStride] = QT(k);
+                cnt += h ? 1u : 0u;
                 total += h ? 1 : 0;
                 done = done || total >= maxHits;
             }
             e += kChunk;
             done = done || e >= n;
         }
-        if (!any || __any_sync(0xFFFFFFFFu, cnt > Q - kChunk)) {
-            for (int j = 0; j < cnt; ++j) body(q[j * kStride]);
-            cnt = 0;
-            if (!any) break;
-        }
+        const bool walking = __any_sync(0xFFFFFFFFu, !done);
+        // lanes with nothing queued and nothing left to walk do not hold the
+        // others back; a lane still walking with an empty ring walks again
+        const uint32_t k = walking ? __reduce_min_sync(0xFFFFFFFFu, (done && cnt == 0u) ? 0xFFFFFFFFu : cnt)
+                                   : __reduce_max_sync(0xFFFFFFFFu, cnt);
+        for (uint32_t j = 0; j < k; ++j)
+            if (j < cnt) body(q[((head + j) & uint32_t(Q - 1)) * kStride]);
+        const uint32_t m = min(k, cnt);
+        head += m;
+        cnt -= m;
+        if (!walking) break;
     }
 }
 
