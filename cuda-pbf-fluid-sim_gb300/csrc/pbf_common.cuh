@@ -303,47 +303,90 @@ struct ListSource {
     uint32_t fill;
 };
 
+// Eight list entries held as loaded (one or two 16-byte words), unpacked on use.
+template <class E>
+struct ListChunk;
+template <>
+struct ListChunk<uint32_t> {
+    uint4 a, b;
+    __device__ __forceinline__ void load(const uint32_t* __restrict__ p) {
+        a = __ldg(reinterpret_cast<const uint4*>(p));
+        b = __ldg(reinterpret_cast<const uint4*>(p) + 1);
+    }
+    __device__ __forceinline__ uint32_t get(int u) const {
+        const uint4& w = u < 4 ? a : b;
+        const int v = u & 3;
+        return v == 0 ? w.x : v == 1 ? w.y : v == 2 ? w.z : w.w;
+    }
+};
+template <>
+struct ListChunk<uint16_t> {
+    uint4 a;
+    __device__ __forceinline__ void load(const uint16_t* __restrict__ p) { a = __ldg(reinterpret_cast<const uint4*>(p)); }
+    __device__ __forceinline__ uint32_t get(int u) const {
+        const int v = u >> 1;
+        const uint32_t w = v == 0 ? a.x : v == 1 ? a.y : v == 2 ? a.z : a.w;
+        return (u & 1) ? (w >> 16) : (w & 0xFFFFu);
+    }
+};
+
 // Lockstep walk over a neighbour list.  Each lane keeps its accepted
 // candidates in a ring of Q entries, first in first out, so every particle
 // still sums its neighbours in list order.  A lane walks its next chunk of
-// eight entries while its ring has room for the chunk; after each round the
-// warp runs as many bodies as every lane with work left has queued (all those
-// lanes busy), and once no list is being walked it empties the rings.
+// eight entries while its ring has room for the chunk (the chunk was loaded
+// when the previous one was walked, so its latency hides behind the bodies);
+// after each round the warp runs as many bodies as every lane with work left
+// has queued (all those lanes busy, two at a time so that their independent
+// arithmetic interleaves; each lane still adds its terms in order), and once
+// no list is being walked it empties the rings.
 template <int Q, int kStride, class E, class QT, class Hit, class Body>
 __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E>& src, QT* q, int maxHits,
                                                  Hit&& hit, Body&& body) {
     constexpr int kChunk = 8;
+    constexpr uint32_t kMask = uint32_t(Q - 1);
     static_assert(Q > kChunk && (Q & (Q - 1)) == 0, "the ring holds more than one chunk, a power of two");
     uint32_t head = 0, cnt = 0;
     int total = 0;
     uint32_t e = 0;
     const uint32_t n = src.n;
     bool done = !active || n == 0;
+    ListChunk<E> cur;
+    if (!done) cur.load(src.lst);
     for (;;) {
         if (!done && cnt <= uint32_t(Q - kChunk)) {
-            uint32_t ks[kChunk];
-            load8(src.lst + e, ks);
 #pragma unroll
             for (int u = 0; u < kChunk; ++u) {
                 const bool v = !done && e + uint32_t(u) < n;
-                const uint32_t k = v ? ks[u] : src.fill;
+                const uint32_t k = v ? cur.get(u) : src.fill;
                 const bool h = v && hit(k);
                 // cnt + u < Q: the slot is free (live entries are head .. head + cnt - 1)
-                q[((head + cnt) & uint32_t(Q - 1)) * kStride] = QT(k);
+                q[((head + cnt) & kMask) * kStride] = QT(k);
                 cnt += h ? 1u : 0u;
                 total += h ? 1 : 0;
                 done = done || total >= maxHits;
             }
             e += kChunk;
             done = done || e >= n;
+            if (!done) cur.load(src.lst + e);
         }
         const bool walking = __any_sync(0xFFFFFFFFu, !done);
         // lanes with nothing queued and nothing left to walk do not hold the
         // others back; a lane still walking with an empty ring walks again
         const uint32_t k = walking ? __reduce_min_sync(0xFFFFFFFFu, (done && cnt == 0u) ? 0xFFFFFFFFu : cnt)
                                    : __reduce_max_sync(0xFFFFFFFFu, cnt);
-        for (uint32_t j = 0; j < k; ++j)
-            if (j < cnt) body(q[((head + j) & uint32_t(Q - 1)) * kStride]);
+        if (__all_sync(0xFFFFFFFFu, cnt >= k)) {
+            uint32_t j = 0;
+            for (; j + 2u <= k; j += 2u) {
+                const uint32_t ka = q[((head + j) & kMask) * kStride];
+                const uint32_t kb = q[((head + j + 1u) & kMask) * kStride];
+                body(ka);
+                body(kb);
+            }
+            if (j < k) body(q[((head + j) & kMask) * kStride]);
+        } else {
+            for (uint32_t j = 0; j < k; ++j)
+                if (j < cnt) body(q[((head + j) & kMask) * kStride]);
+        }
         const uint32_t m = min(k, cnt);
         head += m;
         cnt -= m;
