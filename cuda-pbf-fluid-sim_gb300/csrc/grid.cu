@@ -24,19 +24,47 @@ __device__ __forceinline__ uint32_t lower_bound_keys(const uint32_t* __restrict_
 }
 
 constexpr uint32_t kCellsPerThread = 8;
+constexpr uint32_t kLbUnset = 0xFFFFFFFFu;
 
-// One thread per run of 8 consecutive cells: one binary search for the
-// first cell, then a forward walk over the sorted keys.
-__global__ void k_cell_lb(uint32_t* __restrict__ lb, const uint32_t* __restrict__ keys, uint32_t N,
-                          uint32_t numCells) {
-    const uint64_t c0 = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kCellsPerThread;
-    if (c0 > numCells) return;
-    uint32_t p = lower_bound_keys(keys, N, uint32_t(c0));
-    const uint64_t c1 = min(c0 + kCellsPerThread, uint64_t(numCells) + 1u);
-    for (uint64_t c = c0; c < c1; ++c) {
-        while (p < N && __ldg(keys + p) < uint32_t(c)) ++p;
-        lb[c] = p;
+// lb[c] = first sorted slot whose key is >= c, c = 0 .. numCells, in two
+// passes over a table preset to kLbUnset.  Pass one, a thread per slot,
+// writes the cells that have particles: lb[k] = p at the first slot p of key
+// k, and lb[numCells] at the first slot past the grid (N when every key is
+// inside it).
+__global__ void k_cell_lb_mark(uint32_t* __restrict__ lb, const uint32_t* __restrict__ keys, uint32_t N,
+                               uint32_t numCells) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const uint32_t k = keys[p];
+    const uint32_t kp = p > 0 ? keys[p - 1] : 0u;
+    if (k < numCells) {
+        if (p == 0 || kp != k) lb[k] = p;
+        if (p == N - 1) lb[numCells] = N;
+    } else if (p == 0 || kp < numCells) {
+        lb[numCells] = p;
     }
+}
+
+// Pass two, a thread per cell in warps of 32 consecutive cells: an empty cell
+// takes the value of the next cell with particles (no key lies between
+// them); in the warp's window that is a shuffle from the next marked lane,
+// past it one binary search for the first cell after the window.  Lanes past
+// the table count as marked with N, which only matters when N = 0.
+__global__ void k_cell_lb_fill(uint32_t* __restrict__ lb, const uint32_t* __restrict__ keys, uint32_t N,
+                               uint32_t numCells) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t v = c <= numCells ? lb[c] : N;
+    const uint32_t marked = __ballot_sync(0xFFFFFFFFu, v != kLbUnset);
+    const uint32_t after = marked & (0xFFFFFFFFu << lane);  // marked lanes at or after this one
+    uint32_t carry = 0;
+    if (__any_sync(0xFFFFFFFFu, after == 0u)) {
+        const uint32_t cEnd = c - lane + 32u;  // first cell after the window (<= numCells here)
+        if (lane == 0) carry = lower_bound_keys(keys, N, cEnd);
+        carry = __shfl_sync(0xFFFFFFFFu, carry, 0);
+    }
+    const uint32_t next = __shfl_sync(0xFFFFFFFFu, v, int(__ffs(after)) - 1);
+    if (c <= numCells && v == kLbUnset) lb[c] = after ? next : carry;
 }
 
 __global__ void k_cell_ranges_ref(uint32_t* __restrict__ start, uint32_t* __restrict__ end,
@@ -237,8 +265,10 @@ cudaError_t launch_cell_ranges_ref(uint32_t* start, uint32_t* end, const uint32_
 
 cudaError_t launch_cell_lb(uint32_t* lb, const uint32_t* keys_sorted, uint32_t N, uint32_t numCells,
                            cudaStream_t s) {
-    const uint64_t threads = (uint64_t(numCells) + 1u + kCellsPerThread - 1) / kCellsPerThread;
-    k_cell_lb<<<blocks_for(threads, 256), 256, 0, s>>>(lb, keys_sorted, N, numCells);
+    cudaError_t e = cudaMemsetAsync(lb, 0xFF, (size_t(numCells) + 1u) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    if (N > 0) k_cell_lb_mark<<<blocks_for(N, 256), 256, 0, s>>>(lb, keys_sorted, N, numCells);
+    k_cell_lb_fill<<<blocks_for(uint64_t(numCells) + 1u, 256), 256, 0, s>>>(lb, keys_sorted, N, numCells);
     return cudaGetLastError();
 }
 
