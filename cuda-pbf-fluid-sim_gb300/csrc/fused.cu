@@ -289,8 +289,7 @@ __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigne
 // One particle's list being written by a warp: hits of a 32-candidate step
 // are compacted with a ballot into consecutive entries (coalesced stores).
 struct ListWriter {
-    uint32_t* out32;
-    uint16_t* out16;
+    uint32_t* out;  // the particle's list (16-bit entries in staged tiles)
     uint32_t cnt;
     __device__ __forceinline__ void emit(bool in, uint32_t k, uint32_t shift, uint32_t cap, bool staged,
                                          uint32_t lt) {
@@ -298,17 +297,57 @@ struct ListWriter {
         const uint32_t at = cnt + __popc(m & lt);
         if (in && at < cap) {
             if (staged)
-                out16[at] = uint16_t(k + shift);
+                reinterpret_cast<uint16_t*>(out)[at] = uint16_t(k + shift);
             else
-                out32[at] = k;
+                out[at] = k;
         }
         cnt += __popc(m);
     }
 };
 
+// The row walk of the list build for G particles of one cell (G even;
+// particle g emits only when g < used): each candidate is loaded once and
+// tested against the particles two at a time with packed arithmetic.
+template <int G>
+__device__ __forceinline__ void build_rows(const float4* __restrict__ pred, const uint32_t (&sl)[G],
+                                           const float4 (&pp)[G], int used, int nrows, uint32_t rb, uint32_t re,
+                                           uint32_t planShift, float R2, uint32_t cap, bool staged, uint32_t lt,
+                                           uint32_t lane, ListWriter (&w)[G]) {
+    static_assert(G % 2 == 0, "particles are tested in pairs");
+    unsigned long long px[G / 2], py[G / 2], pz[G / 2];
+#pragma unroll
+    for (int h = 0; h < G / 2; ++h) {
+        px[h] = pk2(pp[2 * h].x, pp[2 * h + 1].x);
+        py[h] = pk2(pp[2 * h].y, pp[2 * h + 1].y);
+        pz[h] = pk2(pp[2 * h].z, pp[2 * h + 1].z);
+    }
+    for (int rr = 0; rr < nrows; ++rr) {
+        const uint32_t b = __shfl_sync(0xFFFFFFFFu, rb, rr);
+        const uint32_t e = __shfl_sync(0xFFFFFFFFu, re, rr);
+        // staged tiles have nrows <= 32, so the plan's lane rr is row rr
+        const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, rr);
+#pragma unroll 2
+        for (uint32_t c = b; c < e; c += 32u) {
+            const uint32_t k = c + lane;
+            const bool valid = k < e;
+            const float4 pj = valid ? __ldg(pred + k) : pp[0];
+            const unsigned long long jx = pk2(pj.x, pj.x), jy = pk2(pj.y, pj.y), jz = pk2(pj.z, pj.z);
+#pragma unroll
+            for (int h = 0; h < G / 2; ++h) {
+                // r^2 = rz^2 + (rx^2 + ry^2), as the neighbour passes compute it
+                const unsigned long long dx = sub2(px[h], jx), dy = sub2(py[h], jy), dz = sub2(pz[h], jz);
+                const float2 r2 = upk2(fma2(dz, dz, fma2(dx, dx, mul2(dy, dy))));
+                w[2 * h].emit(valid && k != sl[2 * h] && !(r2.x > R2), k, shift, cap, staged, lt);
+                if (2 * h + 1 < used)
+                    w[2 * h + 1].emit(valid && k != sl[2 * h + 1] && !(r2.y > R2), k, shift, cap, staged, lt);
+            }
+        }
+    }
+}
+
 // Builds the neighbour lists: a warp takes its 32 particles one at a time
-// (two at a time when consecutive particles share a cell, testing both
-// against each candidate with packed arithmetic), 32 candidates per step,
+// (four or two at a time when consecutive particles share a cell, testing
+// them against each candidate with packed arithmetic), 32 candidates per step,
 // and a ballot compacts the candidates within the list radius into the
 // particle's list in walk order (coalesced stores).  Entries are 16-bit
 // stage indices in staged tiles, 32-bit sorted slots otherwise; each warp
@@ -337,7 +376,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     uint32_t cachedKey = 0xFFFFFFFFu, rb = 0, re = 0;
     int nrows = 0;
     bool flat = false;
-    uint32_t T = 0, startOf = 0, ends[8];
+    uint32_t T = 0, startOf = 0, endOf = 0;  // flattened rows: lane r < 9 holds row r's start and end
     float R2 = 0.f;
     for (uint32_t p = 0; p < pend;) {
         const uint32_t s = s0 + p;
@@ -387,25 +426,46 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                 const uint32_t rowSteps = __reduce_add_sync(0xFFFFFFFFu, (len + 31u) >> 5);
                 flat = ((T + 31u) >> 5) * 2u < rowSteps;
                 if (flat) {
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) ends[q] = __shfl_sync(0xFFFFFFFFu, end, q);
+                    endOf = end;
                     startOf = end - len;
                 }
             }
             cachedKey = key;
         }
-        // a second particle of the same cell goes along (the row walk only)
-        const bool pair = !flat && nrows <= 32 && p + 1 < pend && key_s[s + 1] == key;
+        // up to three more particles of the same cell go along (the row walk only)
+        const bool quad = !flat && nrows <= 32 && p + 3 < pend && key_s[s + 3] == key;
+        const bool pair = !flat && nrows <= 32 && !quad && p + 1 < pend && key_s[s + 1] == key;
+        const int used = quad ? 4 : pair ? 2 : 1;
+        if (quad) {
+            uint32_t sl[4];
+            float4 pp[4];
+            ListWriter w[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                sl[g] = s + uint32_t(g);
+                pp[g] = pred[sl[g]];
+                w[g] = ListWriter{list + size_t(sl[g]) * cap, 0u};
+            }
+            build_rows<4>(pred, sl, pp, 4, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                if (lane == 0) count[sl[g]] = w[g].cnt;
+                longest = max(longest, w[g].cnt);
+                overflowed += w[g].cnt > cap ? 1u : 0u;
+            }
+            p += 4u;
+            continue;
+        }
         const uint32_t sB = pair ? s + 1 : s;
         const float4 pa = pred[s], pb = pred[sB];
-        ListWriter wa{list + size_t(s) * cap, reinterpret_cast<uint16_t*>(list + size_t(s) * cap), 0u};
-        ListWriter wb{list + size_t(sB) * cap, reinterpret_cast<uint16_t*>(list + size_t(sB) * cap), 0u};
+        ListWriter wa{list + size_t(s) * cap, 0u};
+        ListWriter wb{list + size_t(sB) * cap, 0u};
         if (flat) {
             for (uint32_t c = 0; c < T; c += 32u) {
                 const uint32_t vi = c + lane;
                 uint32_t row = 0;
 #pragma unroll
-                for (int q = 0; q < 8; ++q) row += (ends[q] <= vi) ? 1u : 0u;
+                for (int q = 0; q < 8; ++q) row += (__shfl_sync(0xFFFFFFFFu, endOf, q) <= vi) ? 1u : 0u;
                 const uint32_t k = __shfl_sync(0xFFFFFFFFu, rb, int(row)) +
                                    (vi - __shfl_sync(0xFFFFFFFFu, startOf, int(row)));
                 const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, int(row));
@@ -417,25 +477,12 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                 wa.emit(in, k, shift, cap, staged, lt);
             }
         } else if (nrows <= 32) {
-            const unsigned long long px = pk2(pa.x, pb.x), py = pk2(pa.y, pb.y), pz = pk2(pa.z, pb.z);
-            for (int rr = 0; rr < nrows; ++rr) {
-                const uint32_t b = __shfl_sync(0xFFFFFFFFu, rb, rr);
-                const uint32_t e = __shfl_sync(0xFFFFFFFFu, re, rr);
-                // staged tiles have nrows <= 32, so the plan's lane rr is row rr
-                const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, rr);
-#pragma unroll 2
-                for (uint32_t c = b; c < e; c += 32u) {
-                    const uint32_t k = c + lane;
-                    const bool valid = k < e;
-                    const float4 pj = valid ? __ldg(pred + k) : pa;
-                    // r^2 = rz^2 + (rx^2 + ry^2), as the neighbour passes compute it
-                    const unsigned long long dx = sub2(px, pk2(pj.x, pj.x)), dy = sub2(py, pk2(pj.y, pj.y)),
-                                             dz = sub2(pz, pk2(pj.z, pj.z));
-                    const float2 r2 = upk2(fma2(dz, dz, fma2(dx, dx, mul2(dy, dy))));
-                    wa.emit(valid && k != s && !(r2.x > R2), k, shift, cap, staged, lt);
-                    if (pair) wb.emit(valid && k != sB && !(r2.y > R2), k, shift, cap, staged, lt);
-                }
-            }
+            const uint32_t sl[2] = {s, sB};
+            const float4 pp[2] = {pa, pb};
+            ListWriter w[2] = {wa, wb};
+            build_rows<2>(pred, sl, pp, used, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
+            wa = w[0];
+            wb = w[1];
         } else {
             // reach > 2: rows in batches of 32, one particle at a time
             const int reach = neighbour_reach(dp);
