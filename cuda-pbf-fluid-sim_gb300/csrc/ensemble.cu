@@ -331,7 +331,8 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
 int pbf_ensemble_launches_per_step(pbf_ensemble* e) {
     if (!e) return 0;
     const int sortPasses = (e->keyBits + 7) / 8;
-    return 1 /*predict_keys*/ + 1 /*hist*/ + sortPasses + 1 /*gather*/ + 1 /*lb*/ + (e->nbrCap ? 1 : 0) /*lists*/ +
+    return 1 /*predict_keys*/ + 1 /*hist*/ + sortPasses + 1 /*gather*/ + (e->N > 0 ? 2 : 1) /*lb mark, fill*/ +
+           (e->nbrCap ? 1 : 0) /*lists*/ +
            2 * e->passes + 1 /*commit*/;
 }
 

@@ -402,7 +402,7 @@ bool Simulator::step(const SimParams& p) {
 
 int Simulator::launchesPerStep() const {
     const int passes = (m_grid.keyBits + 7) / 8;
-    int n = 1 /*predict_keys*/ + 1 /*hist*/ + passes + 1 /*gather*/ + 1 /*lb*/;
+    int n = 1 /*predict_keys*/ + 1 /*hist*/ + passes + 1 /*gather*/ + (m_params.numParticles > 0 ? 2 : 1) /*lb mark, fill*/;
     if (m_grid.hashed) n += 1;
     n += (m_params.solverIters > 0) ? 2 * m_params.solverIters : 1;
     if (m_bufs.nbrListCap > 0) n += pbf::fused_list_builds(fused_shape(m_bufs, m_grid, m_params));
