@@ -113,6 +113,16 @@ def alg_bytes_per_particle(phase: str, n: int, num_cells: int, hashed: bool, ite
     return 0.0
 
 
+def tuning_report(lib, chosen, ms, steps, api):
+    """The autotuner's choice and the per-shape step times it measured."""
+    import pbfx
+    shapes = pbfx.tile_shapes(lib)
+    return {"shape": chosen, "tile": shapes[chosen][0], "stage_slots": shapes[chosen][1],
+            "ms_per_step": {"%d/%d" % sh: round(m, 4) for sh, m in zip(shapes, ms)},
+            "what": "%s: every tile shape (particles per CTA / staged slots) timed over %d steps from the "
+                    "post-warm-up state, state restored, untimed" % (api, steps)}
+
+
 def issue_peak(clk) -> float:
     """Warp instructions per second the GPU can issue: 4 schedulers per SM."""
     import torch
@@ -313,6 +323,10 @@ def run_ours(args, cfg, world, rank, local):
     for _ in range(args.warmup):
         pbfx.check(lib.pbf_step(sim.h, pp))
     pbfx.check(lib.pbf_synchronize(sim.h))
+    tuned = None
+    if args.autotune_steps > 0:  # untimed; the tuner puts the state back
+        tuned = tuning_report(lib, *sim.autotune(steps=args.autotune_steps, params=p), args.autotune_steps,
+                              "pbf_autotune_tile_shape")
     snap_pos, snap_vel = sim.download()  # state at the start of the timed region
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -407,6 +421,7 @@ def run_ours(args, cfg, world, rank, local):
         "step_ms": {"first": round(step_ms[0], 4), "median": round(statistics.median(step_ms), 4),
                     "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
         "gpu_launches": launches,
+        "autotune": tuned,
         "clocks": clk,
         "neighbour_lists": {"capacity": list_cap, "longest": list_longest, "overflowed": list_overflowed},
     }
@@ -561,6 +576,10 @@ def run_ensemble(args, cfg, world, rank, local):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     pbfx.check(lib.pbf_ensemble_step(ens.h, args.warmup))
     pbfx.check(lib.pbf_ensemble_synchronize(ens.h))
+    tuned = None
+    if args.autotune_steps > 0:  # untimed; the tuner puts the state back
+        tuned = tuning_report(lib, *ens.autotune(steps=args.autotune_steps), args.autotune_steps,
+                              "pbf_ensemble_autotune")
     snap_pos, snap_vel = ens.download()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = ClockSampler()
@@ -663,6 +682,7 @@ def run_ensemble(args, cfg, world, rank, local):
         "step_ms": {"first": round(step_ms[0], 4), "median": round(statistics.median(step_ms), 4),
                     "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
         "gpu_launches": launches,
+        "autotune": tuned,
         "clocks": clk,
     }
 
@@ -697,6 +717,8 @@ def main(argv=None):
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--autotune-steps", type=int, default=3,
+                    help="steps per tile shape for the autotuner after warm-up (0: keep the default shape)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     ap.add_argument("--profile-steps", type=int, default=5)

@@ -428,6 +428,39 @@ int pbf_set_neighbour_list_capacity(pbf_sim* h, uint32_t entries) {
     return PBF_OK;
 }
 
+int pbf_tile_shape_count(void) { return pbf::fused_tile_shape_count(); }
+
+int pbf_tile_shape_info(int id, int* tile, int* stage_slots) {
+    int t = 0, st = 0;
+    if (!pbf::fused_tile_shape_info(id, t, st)) return PBF_ERR_INVALID;
+    if (tile) *tile = t;
+    if (stage_slots) *stage_slots = st;
+    return PBF_OK;
+}
+
+int pbf_set_tile_shape(pbf_sim* h, int id) {
+    if (!h || !h->sim.setTileShape(id)) return PBF_ERR_INVALID;
+    return PBF_OK;
+}
+
+int pbf_get_tile_shape(pbf_sim* h, int* id) {
+    if (!h || !id) return PBF_ERR_INVALID;
+    *id = h->sim.tileShape();
+    return PBF_OK;
+}
+
+int pbf_autotune_tile_shape(pbf_sim* h, const pbf_sim_params* p, int steps, float* ms, int* chosen) {
+    if (!h || steps < 1) return PBF_ERR_INVALID;
+    const sim::SimParams& sp = p ? S(p) : h->sim.params();
+    if (sp.solverIters < 0 || !(sp.grid.cellSize > 0.f)) return PBF_ERR_INVALID;
+    if (!h->sim.autotuneTileShape(sp, steps, ms)) {
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? PBF_ERR_INVALID : from_cuda(e);
+    }
+    if (chosen) *chosen = h->sim.tileShape();
+    return PBF_OK;
+}
+
 int pbf_neighbour_list_stats(pbf_sim* h, uint32_t* capacity, uint32_t* longest, uint32_t* overflowed, int reset) {
     if (!h) return PBF_ERR_INVALID;
     uint32_t l = 0, o = 0;

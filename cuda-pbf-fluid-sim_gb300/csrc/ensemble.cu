@@ -98,6 +98,7 @@ struct pbf_ensemble {
     uint32_t *keys = nullptr, *key_s = nullptr, *perm = nullptr, *lb = nullptr, *sceneOfId = nullptr,
              *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr;
     uint32_t nbrCap = 0;
+    int tile = 0;  // tile shape of the list passes
     pbf::SceneInfo* scenes = nullptr;
     void* sortTemp = nullptr;
     size_t sortBytes = 0;
@@ -137,6 +138,7 @@ struct pbf_ensemble {
         m.nbr_stats = nbrStats;
         m.nbr_cap = nbrCap;
         m.err = err;
+        m.tile = tile;
         return m;
     }
 
@@ -176,6 +178,18 @@ struct pbf_ensemble {
         }
         graph = gr;
         return pbf::from_cuda(cudaGraphUpload(exec, stream));
+    }
+
+    // Replaces the step graph with one for tile shape `id`.
+    int set_tile(int id) {
+        if (id == tile && exec) return PBF_OK;
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return PBF_ERR_CUDA;
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        tile = id;
+        return capture();
     }
 };
 
@@ -326,6 +340,69 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
         return (err & pbf::kErrNonFiniteBit) ? PBF_ERR_NONFINITE : PBF_ERR_CUDA;
     }
     return PBF_OK;
+}
+
+int pbf_ensemble_set_tile_shape(pbf_ensemble* e, int id) {
+    if (!e || id < 0 || id >= pbf::fused_tile_shape_count()) return PBF_ERR_INVALID;
+    return e->set_tile(id);
+}
+
+int pbf_ensemble_get_tile_shape(pbf_ensemble* e, int* id) {
+    if (!e || !id) return PBF_ERR_INVALID;
+    *id = e->tile;
+    return PBF_OK;
+}
+
+// Every shape is timed from the same state (one untimed step first, which
+// also loads the graph); the state is put back afterwards.
+int pbf_ensemble_autotune(pbf_ensemble* e, int steps, float* ms, int* chosen) {
+    if (!e || steps < 1) return PBF_ERR_INVALID;
+    const int shapes = pbf::fused_tile_shape_count();
+    const int before = e->tile;
+    const size_t bytes = sizeof(float4) * size_t(e->N);
+    float4* snap = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int st = PBF_OK;
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess ||
+        cudaMalloc(&snap, 2 * std::max<size_t>(bytes, 16)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess ||
+        cudaMemcpyAsync(snap, e->pos, bytes, cudaMemcpyDeviceToDevice, e->stream) != cudaSuccess ||
+        cudaMemcpyAsync(snap + e->N, e->vel, bytes, cudaMemcpyDeviceToDevice, e->stream) != cudaSuccess)
+        st = PBF_ERR_CUDA;
+    auto restore = [&]() {
+        return cudaMemcpyAsync(e->pos, snap, bytes, cudaMemcpyDeviceToDevice, e->stream) == cudaSuccess &&
+               cudaMemcpyAsync(e->vel, snap + e->N, bytes, cudaMemcpyDeviceToDevice, e->stream) == cudaSuccess;
+    };
+    int best = before;
+    float bestMs = 0.f;
+    for (int id = 0; st == PBF_OK && id < shapes; ++id) {
+        if ((st = e->set_tile(id)) != PBF_OK) break;
+        bool ok = cudaGraphLaunch(e->exec, e->stream) == cudaSuccess && restore() &&
+                  cudaEventRecord(e0, e->stream) == cudaSuccess;
+        for (int i = 0; ok && i < steps; ++i) ok = cudaGraphLaunch(e->exec, e->stream) == cudaSuccess;
+        float t = 0.f;
+        ok = ok && cudaEventRecord(e1, e->stream) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+             cudaEventElapsedTime(&t, e0, e1) == cudaSuccess && restore();
+        if (!ok) {
+            st = PBF_ERR_CUDA;
+            break;
+        }
+        t /= float(steps);
+        if (ms) ms[id] = t;
+        if (id == 0 || t < bestMs) {
+            best = id;
+            bestMs = t;
+        }
+    }
+    if (snap && !(restore() && cudaStreamSynchronize(e->stream) == cudaSuccess) && st == PBF_OK) st = PBF_ERR_CUDA;
+    const int st2 = e->set_tile(st == PBF_OK ? best : before);
+    if (st == PBF_OK) st = st2;
+    if (e->nbrStats) cudaMemset(e->nbrStats, 0, 2 * sizeof(uint32_t));
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (snap) cudaFree(snap);
+    if (st == PBF_OK && chosen) *chosen = e->tile;
+    return st;
 }
 
 int pbf_ensemble_launches_per_step(pbf_ensemble* e) {

@@ -101,21 +101,49 @@ __device__ __forceinline__ bool scene_lists(const SceneView& v, const ListBufs& 
 }
 
 // ------------------------------------------------------------- tiles
-// The list passes work on tiles of kTile consecutive sorted slots, one CTA
+// The list passes work on tiles of Sh::kTile consecutive sorted slots, one CTA
 // per tile.  When the tile's particles all lie in one scene and one (y, z)
 // row of cells, the union of their stencils is (2 reach + 1)^2 rows of
 // cells, each one contiguous slot range [start, start + len) covering the
-// tile's x range widened by reach.  If those ranges hold at most kStageMax
-// slots, the tile is "staged": every list pass copies the ranges into shared
+// tile's x range widened by reach.  If those ranges hold at most
+// Sh::kStageMax slots, the tile is "staged": every list pass copies the ranges into shared
 // memory (row r at base[r]) and the lists of its particles hold 16-bit
 // indices into that copy, so neighbour reads are shared-memory gathers.
 // Other tiles' lists hold 32-bit sorted slots read from global memory.  The
 // plan depends only on the sorted keys, the lower-bound table and the
 // scenes, so the list builder and every list pass derive the same one.
-constexpr int kTile = kNbrBS;
-constexpr int kStageMax = 1536;
 constexpr int kPlanRows = 32;
-static_assert(kStageMax <= 65536, "staged indices are 16-bit");
+
+// A tile shape the list passes (and the list build, which must plan the same
+// tiles) are compiled for: slots per tile (= threads per CTA), stage slots,
+// and the CTAs per SM that the shape's shared memory allows, which the launch
+// bounds pass on so that the register budget matches that occupancy.  The
+// shapes give identical results (only which tiles are staged differs); the
+// autotuner picks one by timing.
+//
+// Shared memory of the list passes.  lambda / delta: the stage (kStageMax
+// float4) then a queue of 16-bit stage indices (kQueue x kTile) for staged
+// tiles; tiles that are not staged keep 32-bit queues in the stage area.
+// XSPH: the stage as float4 (x, y, z, vx) plus float2 (vy, vz), its queue in
+// the stage area likewise.  In a staged tile a warp whose lists overflowed
+// walks the stencil in one pass, without a queue.
+template <int T, int S, int MinSolve, int MinCommit>
+struct TileShape {
+    static constexpr int kTile = T;
+    static constexpr int kStageMax = S;
+    static constexpr int kMinSolve = MinSolve;
+    static constexpr int kMinCommit = MinCommit;
+    static constexpr size_t kStageBytes = size_t(S) * sizeof(float4);
+    static constexpr size_t kSolveSmem = kStageBytes + size_t(kQueue) * T * sizeof(uint16_t);
+    static constexpr size_t kCommitSmem = kStageBytes + size_t(S) * sizeof(float2);
+    static_assert(T % 32 == 0 && T <= 1024, "tiles are whole warps of one CTA");
+    static_assert(S <= 32768, "staged indices are 16-bit");
+    static_assert(size_t(kQueue) * T * sizeof(uint32_t) <= kStageBytes, "32-bit queues fit in the stage area");
+};
+using TileShape0 = TileShape<128, 1536, 6, 6>;
+using TileShape1 = TileShape<64, 1024, 10, 8>;
+using TileShape2 = TileShape<128, 2048, 5, 4>;
+using TileShape3 = TileShape<256, 3072, 3, 3>;
 
 struct TilePlan {
     uint32_t start[kPlanRows];
@@ -137,11 +165,11 @@ struct WarpPlan {
     bool lists;
 };
 
-template <class Scenes>
+template <class Sh, class Scenes>
 __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                    const Scenes& S, const ListBufs& lbuf, uint32_t t0, uint32_t N) {
     const int lane = int(threadIdx.x & 31u);
-    const uint32_t tl = min(t0 + uint32_t(kTile), N) - 1u;
+    const uint32_t tl = min(t0 + uint32_t(Sh::kTile), N) - 1u;
     const SceneView v = S.view(t0);
     const sim::DeviceParams& dp = *v.dp;
     const int3 dim = dp.grid.dim;
@@ -176,15 +204,15 @@ __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uin
     }
     w.total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     w.base = incl - w.len;
-    w.staged = single && w.total <= uint32_t(kStageMax);
+    w.staged = single && w.total <= uint32_t(Sh::kStageMax);
     return w;
 }
 
 // The plan in shared memory for a CTA (written by warp 0).
-template <class Scenes>
+template <class Sh, class Scenes>
 __device__ void plan_tile(TilePlan& P, const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                           const Scenes& S, const ListBufs& lbuf, uint32_t t0, uint32_t N) {
-    const WarpPlan w = plan_tile_warp(key_s, lb, S, lbuf, t0, N);
+    const WarpPlan w = plan_tile_warp<Sh>(key_s, lb, S, lbuf, t0, N);
     const int lane = int(threadIdx.x & 31u);
     P.start[lane] = w.start;
     P.base[lane] = w.base;
@@ -221,12 +249,13 @@ __device__ __forceinline__ RowSource row_source(const uint32_t* __restrict__ key
 // with w = lam[k] when lam is given; with vel given, w = vel[k].x and
 // sv[i] = (vel[k].y, vel[k].z).  Every thread of the CTA calls it (between
 // barriers).
+template <class Sh>
 __device__ __forceinline__ void stage_tile(const TilePlan& P, const float4* __restrict__ pos,
                                            const float* __restrict__ lam, const float4* __restrict__ vel,
                                            float4* sp, float2* sv) {
     for (int r = 0; r < P.nrows; ++r) {
         const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
-        for (uint32_t i = threadIdx.x; i < len; i += kTile) {
+        for (uint32_t i = threadIdx.x; i < len; i += Sh::kTile) {
             float4 x = __ldg(pos + st + i);
             if (lam) x.w = __ldg(lam + st + i);
             if (vel) {
@@ -242,17 +271,17 @@ __device__ __forceinline__ void stage_tile(const TilePlan& P, const float4* __re
 // Plans the CTA's tile and stages it when it is staged and its scene has
 // lists; returns whether the tile is staged.  CTA-uniform; every thread
 // calls it.
-template <class Scenes>
+template <class Sh, class Scenes>
 __device__ __forceinline__ bool plan_and_stage(TilePlan& P, const uint32_t* __restrict__ key_s,
                                                const uint32_t* __restrict__ lb, const Scenes& S,
                                                const ListBufs& lbuf, uint32_t t0, uint32_t N,
                                                const float4* __restrict__ pos, const float* __restrict__ lam,
                                                const float4* __restrict__ vel, float4* sp, float2* sv) {
     if (lbuf.cap == 0) return false;
-    if (threadIdx.x < 32) plan_tile(P, key_s, lb, S, lbuf, t0, N);
+    if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N);
     __syncthreads();
     const bool staged = P.staged && P.lists && lbuf.staging;
-    if (staged) stage_tile(P, pos, lam, vel, sp, sv);
+    if (staged) stage_tile<Sh>(P, pos, lam, vel, sp, sv);
     __syncthreads();
     return staged;
 }
@@ -355,8 +384,7 @@ __device__ __forceinline__ void build_rows(const float4* __restrict__ pred, cons
 // consecutive particles share a cell.  A particle whose scene has no lists
 // gets the count cap + 1 (its warp walks the stencil).
 constexpr int kBuildBS = 256;
-static_assert(kTile % 32 == 0, "tiles are whole warps");
-template <class Scenes>
+template <class Scenes, class Sh>
 __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restrict__ pred,
                                                           const uint32_t* __restrict__ key_s,
                                                           const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
@@ -366,7 +394,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     const uint32_t s0 = (blockIdx.x * kBuildBS + threadIdx.x) & ~31u;
     if (s0 >= N) return;  // warp-uniform
     const uint32_t cap = lbuf.cap;
-    const WarpPlan plan = plan_tile_warp(key_s, lb, S, lbuf, s0 - s0 % uint32_t(kTile), N);
+    const WarpPlan plan = plan_tile_warp<Sh>(key_s, lb, S, lbuf, s0 - s0 % uint32_t(Sh::kTile), N);
     const bool staged = plan.staged && lbuf.staging;
     const uint32_t planShift = plan.base - plan.start;  // lane r: stage index of slot k in row r is k + shift
     const uint32_t lt = lanemask_lt();
@@ -534,34 +562,23 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     }
 }
 
-// Shared memory of the list passes.  lambda / delta: the stage (kStageMax
-// float4) then a queue of 16-bit stage indices (kQueue x kTile) for staged
-// tiles; tiles that are not staged keep 32-bit queues in the stage area.
-// XSPH: the stage as float4 (x, y, z, vx) plus float2 (vy, vz), its queue in
-// the stage area likewise.  In a staged tile a warp whose lists overflowed
-// walks the stencil in one pass, without a queue.
-constexpr size_t kStageBytes = size_t(kStageMax) * sizeof(float4);
-constexpr size_t kSolveSmem = kStageBytes + size_t(kQueue) * kTile * sizeof(uint16_t);
-constexpr size_t kCommitSmem = kStageBytes + size_t(kStageMax) * sizeof(float2);
-static_assert(size_t(kQueue) * kTile * sizeof(uint32_t) <= kStageBytes, "32-bit queues fit in the stage area");
-
 // lambda of iteration `it` for every slot whose scene runs that iteration.
-template <class Scenes>
-__global__ void __launch_bounds__(kTile, 6) k_lambda(int it, const float4* __restrict__ pred,
+template <class Scenes, class Sh>
+__global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
-    uint16_t* q16 = reinterpret_cast<uint16_t*>(smem + kStageMax) + threadIdx.x;
+    uint16_t* q16 = reinterpret_cast<uint16_t*>(smem + Sh::kStageMax) + threadIdx.x;
     uint32_t* q32 = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
-    const uint32_t t0 = blockIdx.x * kTile;
+    const uint32_t t0 = blockIdx.x * Sh::kTile;
     const uint32_t s = t0 + threadIdx.x;
     const uint32_t sc = s < N ? s : 0u;
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, nullptr, sp, nullptr);
+    const bool staged = plan_and_stage<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, nullptr, sp, nullptr);
     const float4 pi = pred[sc];
     const GlobalData g{pred, nullptr, nullptr};
     uint32_t n;
@@ -569,11 +586,11 @@ __global__ void __launch_bounds__(kTile, 6) k_lambda(int it, const float4* __res
     if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            l = lambda_queued<kQueue, kTile>(active, sc, pi,
+            l = lambda_queued<kQueue, Sh::kTile>(active, sc, pi,
                                              ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                              StagedData{sp, nullptr}, q16);
         else
-            l = lambda_queued<kQueue, kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
+            l = lambda_queued<kQueue, Sh::kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
     } else if (staged) {
         int cx, cy, cz;
         decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
@@ -583,7 +600,7 @@ __global__ void __launch_bounds__(kTile, 6) k_lambda(int it, const float4* __res
                 return __ldg(pred + k);
             });
     } else {
-        l = lambda_queued<kQueue, kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
+        l = lambda_queued<kQueue, Sh::kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
     }
     if (active) lam[s] = l;
 }
@@ -592,8 +609,8 @@ __global__ void __launch_bounds__(kTile, 6) k_lambda(int it, const float4* __res
 // post-solve boundary (e = 0) and computes v = (x - p)/dt; a scene past its
 // iterations carries its prediction through, and a scene without iterations
 // gets boundary and velocity in pass 0.
-template <class Scenes>
-__global__ void __launch_bounds__(kTile, 6) k_delta(int it, const float4* __restrict__ pred,
+template <class Scenes, class Sh>
+__global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, const float4* __restrict__ pred,
                                                  const float* __restrict__ lam, const uint32_t* __restrict__ key_s,
                                                  const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
                                                  float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
@@ -601,15 +618,15 @@ __global__ void __launch_bounds__(kTile, 6) k_delta(int it, const float4* __rest
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
-    uint16_t* q16 = reinterpret_cast<uint16_t*>(smem + kStageMax) + threadIdx.x;
+    uint16_t* q16 = reinterpret_cast<uint16_t*>(smem + Sh::kStageMax) + threadIdx.x;
     uint32_t* q32 = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
-    const uint32_t t0 = blockIdx.x * kTile;
+    const uint32_t t0 = blockIdx.x * Sh::kTile;
     const uint32_t s = t0 + threadIdx.x;
     const uint32_t sc = s < N ? s : 0u;
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, lam, nullptr, sp, nullptr);
+    const bool staged = plan_and_stage<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, lam, nullptr, sp, nullptr);
     const float4 pi = pred[sc];
     const float lam_i = lam[sc];
     const float w_q = scorr_wq(dp);
@@ -619,11 +636,11 @@ __global__ void __launch_bounds__(kTile, 6) k_delta(int it, const float4* __rest
     if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i,
+            d = delta_queued<kQueue, Sh::kTile>(active, sc, pi, lam_i,
                                             ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                             w_q, StagedData{sp, nullptr}, q16);
         else
-            d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
+            d = delta_queued<kQueue, Sh::kTile>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
                                             q32);
     } else if (staged) {
         int cx, cy, cz;
@@ -636,7 +653,7 @@ __global__ void __launch_bounds__(kTile, 6) k_delta(int it, const float4* __rest
                              return __ldg(pred + k);
                          });
     } else {
-        d = delta_queued<kQueue, kTile>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
+        d = delta_queued<kQueue, Sh::kTile>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
     }
     if (s >= N) return;
     const bool last = active ? it == v.iters - 1 : (v.iters <= 0 && it == 0);
@@ -672,15 +689,15 @@ __global__ void __launch_bounds__(kBS) k_finalize_no_iters(float4* __restrict__ 
 }
 
 // XSPH (Jacobi, where the scene configures it), boundary(e), scatter to ids.
-template <class Scenes, bool kXsph>
-__global__ void __launch_bounds__(kTile, 6) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
+template <class Scenes, bool kXsph, class Sh>
+__global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const float4* __restrict__ pred, const float4* __restrict__ vel_s,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   const uint32_t* __restrict__ perm, Scenes S, uint32_t N,
                                                   float4* __restrict__ pos, float4* __restrict__ vel, ListBufs lbuf,
                                                   uint32_t* __restrict__ err) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
-    const uint32_t t0 = blockIdx.x * kTile;
+    const uint32_t t0 = blockIdx.x * Sh::kTile;
     const uint32_t s = t0 + threadIdx.x;
     const uint32_t sc = s < N ? s : 0u;
     const SceneView v = S.view(sc);
@@ -689,9 +706,9 @@ __global__ void __launch_bounds__(kTile, 6) k_commit(const float4* __restrict__ 
     float4 vv = vel_s[sc];
     if (kXsph) {
         float4* sp = smem;
-        float2* sv = reinterpret_cast<float2*>(smem + kStageMax);
+        float2* sv = reinterpret_cast<float2*>(smem + Sh::kStageMax);
         const bool xs = s < N && dp.xsph_c > 0.f;  // every lane takes part in the warp-wide rounds
-        const bool staged = plan_and_stage(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, vel_s, sp, sv);
+        const bool staged = plan_and_stage<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, vel_s, sp, sv);
         // Queue of the queued walks: the stage area, free in tiles that are
         // not staged.  In a staged tile a warp whose lists overflowed walks
         // the stencil without a queue.
@@ -706,7 +723,7 @@ __global__ void __launch_bounds__(kTile, 6) k_commit(const float4* __restrict__ 
                                       ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                       StagedData{sp, sv});
             else
-                vx = xsph_queued<kQueue, kTile>(xs, sc, x, vv, ListSource<uint32_t>{base, n, sc}, dp, g, q);
+                vx = xsph_queued<kQueue, Sh::kTile>(xs, sc, x, vv, ListSource<uint32_t>{base, n, sc}, dp, g, q);
         } else if (staged) {
             int cx, cy, cz;
             decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
@@ -718,7 +735,7 @@ __global__ void __launch_bounds__(kTile, 6) k_commit(const float4* __restrict__ 
                                  return __ldg(pred + k);
                              });
         } else {
-            vx = xsph_queued<kQueue, kTile>(xs, sc, x, vv, row_source(key_s, lb, v, sc), dp, g, q);
+            vx = xsph_queued<kQueue, Sh::kTile>(xs, sc, x, vv, row_source(key_s, lb, v, sc), dp, g, q);
         }
         if (xs) vv = vx;
     }
@@ -909,8 +926,53 @@ int fused_list_builds(const FusedShape& sh) {
     return (sh.iters + sh.list_span - 1) / sh.list_span;
 }
 
-// Opts the list passes into their dynamic shared memory (above the 48 KB
-// default); once per process and device, before the first launch or capture.
+namespace {
+
+// Calls f with the tile shape `id` names (an unknown id takes shape 0).
+template <class F>
+cudaError_t with_tile_shape(int id, F&& f) {
+    switch (id) {
+    case 1: return f(TileShape1{});
+    case 2: return f(TileShape2{});
+    case 3: return f(TileShape3{});
+    default: return f(TileShape0{});
+    }
+}
+
+template <class Sh>
+cudaError_t prepare_shape() {
+    const int solve = int(Sh::kSolveSmem), commit = int(Sh::kCommitSmem);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_lambda<OneScene, Sh>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_lambda<ManyScenes, Sh>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<OneScene, Sh>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<ManyScenes, Sh>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<OneScene, true, Sh>, a, commit)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<OneScene, false, Sh>, a, commit)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_commit<ManyScenes, true, Sh>, a, commit)) != cudaSuccess)
+        return e;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+int fused_tile_shape_count() { return kTileShapeCount; }
+
+bool fused_tile_shape_info(int id, int& tile, int& stage) {
+    if (id < 0 || id >= kTileShapeCount) return false;
+    with_tile_shape(id, [&](auto shape) {
+        using Sh = decltype(shape);
+        tile = Sh::kTile;
+        stage = Sh::kStageMax;
+        return cudaSuccess;
+    });
+    return true;
+}
+
+// Opts the list passes of every tile shape into their dynamic shared memory
+// (above the 48 KB default); once per process and device, before the first
+// launch or capture.
 cudaError_t fused_prepare_kernels() {
     static std::mutex mu;
     static bool done[64] = {};
@@ -920,15 +982,8 @@ cudaError_t fused_prepare_kernels() {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(mu);
     if (done[dev]) return cudaSuccess;
-    const int solve = int(kSolveSmem), commit = int(kCommitSmem);
-    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    if ((e = cudaFuncSetAttribute(k_lambda<OneScene>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_lambda<ManyScenes>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<OneScene>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<ManyScenes>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_commit<OneScene, true>, a, commit)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_commit<OneScene, false>, a, commit)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_commit<ManyScenes, true>, a, commit)) != cudaSuccess)
+    if ((e = prepare_shape<TileShape0>()) != cudaSuccess || (e = prepare_shape<TileShape1>()) != cudaSuccess ||
+        (e = prepare_shape<TileShape2>()) != cudaSuccess || (e = prepare_shape<TileShape3>()) != cudaSuccess)
         return e;
     done[dev] = true;
     return cudaSuccess;
@@ -937,36 +992,42 @@ cudaError_t fused_prepare_kernels() {
 cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, cudaStream_t s) {
     if (sh.N == 0 || !lists_on(b, sh) || it < 0 || it >= sh.iters || it % sh.list_span != 0) return cudaErrorNotReady;
     const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
-    k_build_lists<<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N,
-                                                                 list_bufs(b, sh), b.nbr_list, b.nbr_count,
-                                                                 b.nbr_stats);
-    return cudaGetLastError();
+    return with_tile_shape(sh.tile, [&](auto shape) {
+        using Sh = decltype(shape);
+        k_build_lists<OneScene, Sh><<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(
+            cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N, list_bufs(b, sh), b.nbr_list, b.nbr_count, b.nbr_stats);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, int which, cudaStream_t s) {
     if (sh.N == 0 || it < 0 || it >= sh.iters) return cudaSuccess;
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
-    const unsigned g = blocks_for(sh.N, kTile);
     // iteration it reads buffer (it even ? a : b) and writes the other one
     float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
     float4* nxt = (it % 2 == 0) ? b.pred_b : b.pred_a;
     const OneScene sc = one_scene(b, sh, it);
-    if (which == 0)
-        k_lambda<<<g, kTile, kSolveSmem, s>>>(it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh));
-    else
-        k_delta<<<g, kTile, kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s,
-                                            list_bufs(b, sh));
-    return cudaGetLastError();
+    return with_tile_shape(sh.tile, [&](auto shape) {
+        using Sh = decltype(shape);
+        const unsigned g = blocks_for(sh.N, Sh::kTile);
+        if (which == 0)
+            k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s,
+                                                                         list_bufs(b, sh));
+        else
+            k_delta<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt,
+                                                                        b.pos_s, b.vel_s, list_bufs(b, sh));
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t fused_solve(const FusedBufs& b, const FusedShape& sh, cudaStream_t s) {
     if (sh.N == 0) return cudaSuccess;
     for (int it = 0; it < sh.iters; ++it) {
-        const cudaError_t e = fused_build_lists(b, sh, it, s);
+        cudaError_t e = fused_build_lists(b, sh, it, s);
         if (e != cudaSuccess && e != cudaErrorNotReady) return e;
-        fused_solve_phase(b, sh, it, 0, s);
-        fused_solve_phase(b, sh, it, 1, s);
+        if ((e = fused_solve_phase(b, sh, it, 0, s)) != cudaSuccess) return e;
+        if ((e = fused_solve_phase(b, sh, it, 1, s)) != cudaSuccess) return e;
     }
     if (sh.iters <= 0)
         k_finalize_no_iters<<<blocks_for(sh.N, kBS), kBS, 0, s>>>(b.pred_a, b.pos_s, b.dp, sh.N, b.vel_s);
@@ -978,42 +1039,53 @@ cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t 
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
     const float4* x = fused_final_pred(b, sh);
-    const unsigned g = blocks_for(sh.N, kTile);
     const OneScene sc = one_scene(b, sh, sh.iters);
     const ListBufs lb = list_bufs(b, sh);
-    if (sh.xsph)
-        k_commit<OneScene, true><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc, sh.N, b.pos,
-                                                             b.vel, lb, b.err);
-    else
-        k_commit<OneScene, false><<<g, kTile, kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc, sh.N, b.pos,
-                                                              b.vel, lb, b.err);
-    return cudaGetLastError();
+    return with_tile_shape(sh.tile, [&](auto shape) {
+        using Sh = decltype(shape);
+        const unsigned g = blocks_for(sh.N, Sh::kTile);
+        if (sh.xsph)
+            k_commit<OneScene, true, Sh><<<g, Sh::kTile, Sh::kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc,
+                                                                                sh.N, b.pos, b.vel, lb, b.err);
+        else
+            k_commit<OneScene, false, Sh><<<g, Sh::kTile, Sh::kCommitSmem, s>>>(x, b.vel_s, b.key_s, b.lb, b.perm, sc,
+                                                                                 sh.N, b.pos, b.vel, lb, b.err);
+        return cudaGetLastError();
+    });
 }
 
 // ------------------------------------------------------------ many scenes
 cudaError_t multi_build_lists(const MultiBufs& m, cudaStream_t s) {
     if (m.N == 0 || m.nbr_cap == 0) return cudaSuccess;
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
-    k_build_lists<<<blocks_for(m.N, kBuildBS), kBuildBS, 0, s>>>(m.pred_a, m.key_s, m.lb,
-                                                                ManyScenes{m.scenes, m.sceneOfSlot}, m.N, lb,
-                                                                m.nbr_list, m.nbr_count, m.nbr_stats);
-    return cudaGetLastError();
+    return with_tile_shape(m.tile, [&](auto shape) {
+        using Sh = decltype(shape);
+        k_build_lists<ManyScenes, Sh><<<blocks_for(m.N, kBuildBS), kBuildBS, 0, s>>>(
+            m.pred_a, m.key_s, m.lb, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, lb, m.nbr_list, m.nbr_count,
+            m.nbr_stats);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_t s) {
     if (m.N == 0) return cudaSuccess;
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
-    const unsigned g = blocks_for(m.N, kTile);
     float4* cur = (it % 2 == 0) ? m.pred_a : m.pred_b;
     float4* nxt = (it % 2 == 0) ? m.pred_b : m.pred_a;
     const ManyScenes sc{m.scenes, m.sceneOfSlot};
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
-    if (which == 0)
-        k_lambda<<<g, kTile, kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N, m.lam_s, lb);
-    else
-        k_delta<<<g, kTile, kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N, nxt, m.pos_s, m.vel_s, lb);
-    return cudaGetLastError();
+    return with_tile_shape(m.tile, [&](auto shape) {
+        using Sh = decltype(shape);
+        const unsigned g = blocks_for(m.N, Sh::kTile);
+        if (which == 0)
+            k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N, m.lam_s,
+                                                                           lb);
+        else
+            k_delta<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N,
+                                                                          nxt, m.pos_s, m.vel_s, lb);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStream_t s) {
@@ -1021,10 +1093,13 @@ cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStrea
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
-    k_commit<ManyScenes, true><<<blocks_for(m.N, kTile), kTile, kCommitSmem, s>>>(
-        final_pred, m.vel_s, m.key_s, m.lb, m.perm, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, m.pos, m.vel, lb,
-        m.err);
-    return cudaGetLastError();
+    return with_tile_shape(m.tile, [&](auto shape) {
+        using Sh = decltype(shape);
+        k_commit<ManyScenes, true, Sh><<<blocks_for(m.N, Sh::kTile), Sh::kTile, Sh::kCommitSmem, s>>>(
+            final_pred, m.vel_s, m.key_s, m.lb, m.perm, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, m.pos, m.vel, lb,
+            m.err);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t fused_scatter_lambda(const FusedBufs& b, const FusedShape& sh, float* lambda_by_id, cudaStream_t s) {

@@ -69,7 +69,15 @@ struct FusedShape {
     // lambda of iterations 0, span, 2*span, ...); 0 = every pass walks the
     // stencil.
     int list_span;
+    // Tile shape of the list passes (0 .. fused_tile_shape_count() - 1).
+    int tile;
 };
+
+// Tile shapes the list passes are compiled for: slots per tile (threads per
+// CTA) and slots a tile's stage holds.  Results do not depend on the shape.
+constexpr int kTileShapeCount = 4;
+int fused_tile_shape_count();
+bool fused_tile_shape_info(int id, int& tile, int& stage);
 
 // Iterations a list may cover for these parameters: the list radius grows by
 // 2 * disp_clamp_max_h * h per covered position update; lists are rebuilt
@@ -126,6 +134,7 @@ struct MultiBufs {
     uint32_t *nbr_list, *nbr_count, *nbr_stats;
     uint32_t nbr_cap;  // 0: no lists
     uint32_t* err;     // device error word (kErr* bits)
+    int tile;          // tile shape of the list passes
 };
 
 // The list passes of a batch: lists built once from the prediction (for the

@@ -80,6 +80,7 @@ pbf::FusedShape fused_shape(const DeviceBuffers& b, const GridBuffers& g, const 
     s.hashed = g.hashed;
     s.xsph = b.xsphEnabled;
     s.list_span = pbf::list_span_for(p);
+    s.tile = b.tileShape;
     return s;
 }
 
@@ -408,6 +409,62 @@ int Simulator::launchesPerStep() const {
     if (m_bufs.nbrListCap > 0) n += pbf::fused_list_builds(fused_shape(m_bufs, m_grid, m_params));
     n += 1; /*commit*/
     return n;
+}
+
+bool Simulator::setTileShape(int id) {
+    if (id < 0 || id >= pbf::fused_tile_shape_count()) return false;
+    if (id == m_bufs.tileShape) return true;
+    if (m_stream) cudaStreamSynchronize(m_stream);
+    m_bufs.tileShape = id;
+    m_graphDirty = true;
+    return true;
+}
+
+bool Simulator::autotuneTileShape(const SimParams& p, int steps, float* ms) {
+    if (!m_stream || steps < 1 || p.numParticles > m_bufs.capacity) return false;
+    const uint32_t n = p.numParticles;
+    const int shapes = pbf::fused_tile_shape_count();
+    const int before = m_bufs.tileShape;
+    const uint64_t frame = m_frameIndex;
+    // every shape starts from the state as it is now, and the call leaves it so
+    float4* snap = nullptr;
+    const size_t bytes = sizeof(float4) * size_t(n);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool ok = cudaStreamSynchronize(m_stream) == cudaSuccess &&
+              cudaMalloc(&snap, 2 * std::max<size_t>(bytes, 16)) == cudaSuccess &&
+              cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(snap, m_bufs.d_pos, bytes, cudaMemcpyDeviceToDevice, m_stream) == cudaSuccess &&
+         cudaMemcpyAsync(snap + n, m_bufs.d_vel, bytes, cudaMemcpyDeviceToDevice, m_stream) == cudaSuccess;
+    auto restore = [&]() {
+        return cudaMemcpyAsync(m_bufs.d_pos, snap, bytes, cudaMemcpyDeviceToDevice, m_stream) == cudaSuccess &&
+               cudaMemcpyAsync(m_bufs.d_vel, snap + n, bytes, cudaMemcpyDeviceToDevice, m_stream) == cudaSuccess;
+    };
+    int best = before;
+    float bestMs = 0.f;
+    for (int id = 0; ok && id < shapes; ++id) {
+        // one untimed step captures the shape's graph
+        ok = setTileShape(id) && step(p) && restore() && cudaEventRecord(e0, m_stream) == cudaSuccess;
+        for (int i = 0; ok && i < steps; ++i) ok = step(p);
+        float t = 0.f;
+        ok = ok && cudaEventRecord(e1, m_stream) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+             cudaEventElapsedTime(&t, e0, e1) == cudaSuccess && restore();
+        if (!ok) break;
+        t /= float(steps);
+        if (ms) ms[id] = t;
+        if (id == 0 || t < bestMs) {
+            best = id;
+            bestMs = t;
+        }
+    }
+    if (snap) ok = restore() && cudaStreamSynchronize(m_stream) == cudaSuccess && ok;
+    m_frameIndex = frame;
+    setTileShape(ok ? best : before);
+    uint32_t l = 0, o = 0;
+    neighbourListStats(l, o, true);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (snap) cudaFree(snap);
+    return ok;
 }
 
 bool Simulator::setNeighbourListCapacity(uint32_t entries) {

@@ -169,6 +169,14 @@ _SIGS = {
     "pbf_ensemble_synchronize": ([_VP], _I),
     "pbf_ensemble_launches_per_step": ([_VP], _I),
     "pbf_neighbour_list_stats": ([_VP, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32), _I], _I),
+    "pbf_tile_shape_count": ([], _I),
+    "pbf_tile_shape_info": ([_I, C.POINTER(_I), C.POINTER(_I)], _I),
+    "pbf_set_tile_shape": ([_VP, _I], _I),
+    "pbf_get_tile_shape": ([_VP, C.POINTER(_I)], _I),
+    "pbf_autotune_tile_shape": ([_VP, C.POINTER(SimParams), _I, C.POINTER(_F), C.POINTER(_I)], _I),
+    "pbf_ensemble_set_tile_shape": ([_VP, _I], _I),
+    "pbf_ensemble_get_tile_shape": ([_VP, C.POINTER(_I)], _I),
+    "pbf_ensemble_autotune": ([_VP, _I, C.POINTER(_F), C.POINTER(_I)], _I),
 }
 
 _ORACLE_SIGS = {
@@ -363,6 +371,23 @@ class Sim:
     def set_list_capacity(self, entries: int):
         check(self.lib.pbf_set_neighbour_list_capacity(self.h, entries), "set_neighbour_list_capacity")
 
+    def set_tile_shape(self, shape: int):
+        check(self.lib.pbf_set_tile_shape(self.h, shape), "set_tile_shape")
+
+    def tile_shape(self) -> int:
+        v = _I()
+        check(self.lib.pbf_get_tile_shape(self.h, C.byref(v)), "get_tile_shape")
+        return int(v.value)
+
+    def autotune(self, steps: int = 3, params: SimParams | None = None):
+        """Runs the tile-shape autotuner; returns (chosen shape, ms per step of each shape)."""
+        n = int(self.lib.pbf_tile_shape_count())
+        ms = (_F * n)()
+        chosen = _I()
+        check(self.lib.pbf_autotune_tile_shape(self.h, C.byref(params) if params is not None else None, steps, ms,
+                                               C.byref(chosen)), "autotune_tile_shape")
+        return int(chosen.value), [float(x) for x in ms]
+
     def list_stats(self, reset: bool = False):
         """(capacity, longest list, overflowed lists) since the last reset."""
         c, l, o = _U32(), _U32(), _U32()
@@ -423,6 +448,32 @@ class Ensemble:
 
     def launches_per_step(self) -> int:
         return int(self.lib.pbf_ensemble_launches_per_step(self.h))
+
+    def set_tile_shape(self, shape: int):
+        check(self.lib.pbf_ensemble_set_tile_shape(self.h, shape), "ensemble set_tile_shape")
+
+    def tile_shape(self) -> int:
+        v = _I()
+        check(self.lib.pbf_ensemble_get_tile_shape(self.h, C.byref(v)), "ensemble get_tile_shape")
+        return int(v.value)
+
+    def autotune(self, steps: int = 3):
+        """Runs the tile-shape autotuner; returns (chosen shape, ms per step of each shape)."""
+        n = int(self.lib.pbf_tile_shape_count())
+        ms = (_F * n)()
+        chosen = _I()
+        check(self.lib.pbf_ensemble_autotune(self.h, steps, ms, C.byref(chosen)), "ensemble autotune")
+        return int(chosen.value), [float(x) for x in ms]
+
+
+def tile_shapes(lib):
+    """[(particles per CTA, staged slots)] of the neighbour passes' tile shapes."""
+    out = []
+    for i in range(int(lib.pbf_tile_shape_count())):
+        t, st = _I(), _I()
+        check(lib.pbf_tile_shape_info(i, C.byref(t), C.byref(st)), "tile_shape_info")
+        out.append((int(t.value), int(st.value)))
+    return out
 
 
 def lattice_dims(total: int, box_extent, spacing: float):

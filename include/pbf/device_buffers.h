@@ -43,6 +43,9 @@ struct DeviceBuffers {
     uint32_t* d_nbrCount = nullptr;
     uint32_t* d_nbrStats = nullptr;  // [0] longest list built, [1] overflowed lists
     uint32_t nbrListCap = 0;
+    // Tile shape of the list passes (particles per CTA and staged slots; the
+    // results do not depend on it).
+    int tileShape = 0;
 
     bool allocate(uint32_t cap);
     // (Re)allocates the lists for `capacity` particles; entries is rounded up

@@ -253,6 +253,23 @@ int pbf_set_neighbour_list_capacity(pbf_sim* sim, uint32_t entries);
  * (reset != 0 clears them after reading).  Any output may be NULL. */
 int pbf_neighbour_list_stats(pbf_sim* sim, uint32_t* capacity, uint32_t* longest, uint32_t* overflowed, int reset);
 
+/* Tile shapes of the neighbour passes (no counterpart in the reference): a
+ * CTA takes `tile` consecutive sorted particles and stages up to
+ * `stage_slots` neighbour slots in shared memory.  Every shape computes the
+ * same results; which is fastest depends on the scene.  Shapes are numbered
+ * 0 .. pbf_tile_shape_count() - 1 (0 is the default). */
+int pbf_tile_shape_count(void);
+int pbf_tile_shape_info(int id, int* tile, int* stage_slots);
+/* Selects the shape for the following steps (PBF_ERR_INVALID for an unknown id). */
+int pbf_set_tile_shape(pbf_sim* sim, int id);
+int pbf_get_tile_shape(pbf_sim* sim, int* id);
+/* Autotuner: times `steps` steps of every shape from the current state (one
+ * untimed step per shape first), then restores the state, clears the list
+ * statistics and selects the fastest shape.  ms (pbf_tile_shape_count()
+ * floats, may be NULL) receives each shape's mean step time; *chosen (may be
+ * NULL) the selected shape.  Synchronous. */
+int pbf_autotune_tile_shape(pbf_sim* sim, const pbf_sim_params* p, int steps, float* ms, int* chosen);
+
 /* Density-constraint diagnostics of the committed state, uncapped neighbour
  * sums over the step's cell grid: out[0] = mean |rho_i/rho0 - 1|,
  * out[1] = max |rho_i/rho0 - 1|, out[2] = mean max(rho_i/rho0 - 1, 0),
@@ -300,6 +317,13 @@ int pbf_ensemble_step(pbf_ensemble* ens, int n);
 int pbf_ensemble_step_host(pbf_ensemble* ens, float4* pos, float4* vel);
 int pbf_ensemble_synchronize(pbf_ensemble* ens);
 int pbf_ensemble_launches_per_step(pbf_ensemble* ens);
+/* Tile shape of the ensemble's neighbour passes (see pbf_tile_shape_count)
+ * and its autotuner, as for a single simulation: every shape is timed over
+ * `steps` steps from the current state, the state is restored and the
+ * fastest shape kept (the step graph is re-captured for it). */
+int pbf_ensemble_set_tile_shape(pbf_ensemble* ens, int id);
+int pbf_ensemble_get_tile_shape(pbf_ensemble* ens, int* id);
+int pbf_ensemble_autotune(pbf_ensemble* ens, int steps, float* ms, int* chosen);
 
 /* ----------------------------------------------------------------- adjoint */
 /* Reverse-mode gradients of the step.  No counterpart in the reference.

@@ -123,6 +123,18 @@ public:
     bool neighbourListStats(uint32_t& longest, uint32_t& overflowed, bool reset);
     static constexpr uint32_t kDefaultListCapacity = 512;
 
+    // Tile shape of the list passes (no counterpart in the reference): how
+    // many sorted particles a CTA takes and how many neighbour slots it can
+    // stage in shared memory.  Every shape gives the same results; the fastest
+    // depends on the scene.  setTileShape takes effect at the next step.
+    bool setTileShape(int id);
+    int tileShape() const { return m_bufs.tileShape; }
+    // Times `steps` steps of every tile shape from the current state (after
+    // one untimed step per shape), then puts the state back as it was,
+    // clears the list statistics and keeps the fastest shape.  ms (tile
+    // shape count entries, may be null) receives each shape's mean step time.
+    bool autotuneTileShape(const SimParams& p, int steps, float* ms);
+
 private:
     bool ensureCapacity(uint32_t n);
     bool uploadParamsIfChanged();
