@@ -761,7 +761,7 @@ int pbf_backward(pbf_tape* t, const float4* d_pos_bar, const float4* d_vel_bar, 
     if (e != cudaSuccess) return pbf::status_of(e);
     uint32_t err = 0;
     cudaMemcpy(&err, t->err, sizeof(err), cudaMemcpyDeviceToHost);
-    if (err) return (err & pbf::kErrLookbackTimeoutBit) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
+    if (err) return (err & pbf::kErrTimeoutBits) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
     if (xsph_c_bar) *xsph_c_bar = cb;
     return PBF_OK;
 }

@@ -476,7 +476,7 @@ int pbf_synchronize(pbf_sim* h) {
     cudaError_t e = cudaStreamSynchronize(h->sim.cudaStream());
     if (e != cudaSuccess) return from_cuda(e);
     const uint32_t err = h->sim.takeDeviceError();
-    if (err & pbf::kErrLookbackTimeoutBit) return PBF_ERR_TIMEOUT;
+    if (err & pbf::kErrTimeoutBits) return PBF_ERR_TIMEOUT;
     if (err & pbf::kErrNonFiniteBit) return PBF_ERR_NONFINITE;
     if (err) return PBF_ERR_CUDA;
     return PBF_OK;

@@ -336,7 +336,7 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
     if (cudaMemcpy(&err, e->err, sizeof(err), cudaMemcpyDeviceToHost) != cudaSuccess) return PBF_ERR_CUDA;
     if (err) {
         cudaMemset(e->err, 0, sizeof(uint32_t));
-        if (err & pbf::kErrLookbackTimeoutBit) return PBF_ERR_TIMEOUT;
+        if (err & pbf::kErrTimeoutBits) return PBF_ERR_TIMEOUT;
         return (err & pbf::kErrNonFiniteBit) ? PBF_ERR_NONFINITE : PBF_ERR_CUDA;
     }
     return PBF_OK;

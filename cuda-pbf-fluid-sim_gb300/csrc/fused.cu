@@ -146,6 +146,7 @@ using TileShape2 = TileShape<128, 2048, 5, 4>;
 using TileShape3 = TileShape<256, 3072, 3, 3>;
 
 struct TilePlan {
+    uint64_t bar;  // completes when the staged rows have landed in shared memory
     uint32_t start[kPlanRows];
     uint32_t base[kPlanRows];
     uint32_t len[kPlanRows];
@@ -245,45 +246,79 @@ __device__ __forceinline__ RowSource row_source(const uint32_t* __restrict__ key
     return r;
 }
 
-// Copies the tile's staged ranges into shared memory: sp[i] = (x, y, z, w)
-// with w = lam[k] when lam is given; with vel given, w = vel[k].x and
-// sv[i] = (vel[k].y, vel[k].z).  Every thread of the CTA calls it (between
-// barriers).
+// Plans the CTA's tile and, when it is staged and its scene has lists, starts
+// copying the staged position rows into shared memory (sp[base[r] + i] =
+// pos[start[r] + i]): thread 0 issues one TMA bulk copy per row, completing on
+// the plan's barrier, while the other threads go on with their own loads.
+// Returns whether the tile is staged.  CTA-uniform; every thread calls it,
+// and every thread then calls stage_finish before reading the stage.  With
+// kBulk false nothing is issued and stage_rows fills the stage instead.
+template <class Sh, bool kBulk, class Scenes>
+__device__ __forceinline__ bool plan_and_issue(TilePlan& P, const uint32_t* __restrict__ key_s,
+                                               const uint32_t* __restrict__ lb, const Scenes& S,
+                                               const ListBufs& lbuf, uint32_t t0, uint32_t N,
+                                               const float4* __restrict__ pos, float4* sp) {
+    if (lbuf.cap == 0) return false;
+    if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N);
+    if (kBulk && threadIdx.x == 0) mbar_init(&P.bar, 1);
+    __syncthreads();
+    const bool staged = P.staged && P.lists && lbuf.staging;
+    if (kBulk && staged && threadIdx.x == 0) {
+        // rows are float4 ranges: 16-byte aligned, sizes multiples of 16
+        mbar_arrive_expect_tx(&P.bar, P.total * uint32_t(sizeof(float4)));
+        for (int r = 0; r < P.nrows; ++r)
+            if (P.len[r]) bulk_copy_g2s(sp + P.base[r], pos + P.start[r], P.len[r] * uint32_t(sizeof(float4)), &P.bar);
+    }
+    return staged;
+}
+
+// Waits (bounded) for the staged rows, then fills in the rest of the stage:
+// w = lam[k] when lam is given; with vel given, w = vel[k].x and sv[i] =
+// (vel[k].y, vel[k].z).  A wait that gives up sets kErrStageTimeoutBit and
+// waits once more (also bounded) so that no copy is still landing when the
+// tile moves on.  CTA-uniform; every thread calls it.
+// The delta pass stages (x, y, z, lambda): a bulk copy of the positions
+// would need a second pass over the stage for lambda once it has landed, and
+// that measured slower than loading both in one pass, as here (sp[base[r] +
+// i] = (pos[k].xyz, lam[k]), k = start[r] + i), followed by a barrier.
 template <class Sh>
-__device__ __forceinline__ void stage_tile(const TilePlan& P, const float4* __restrict__ pos,
-                                           const float* __restrict__ lam, const float4* __restrict__ vel,
-                                           float4* sp, float2* sv) {
+__device__ __forceinline__ void stage_rows(const TilePlan& P, bool staged, const float4* __restrict__ pos,
+                                           const float* __restrict__ lam, float4* sp) {
+    if (!staged) return;
     for (int r = 0; r < P.nrows; ++r) {
         const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
         for (uint32_t i = threadIdx.x; i < len; i += Sh::kTile) {
             float4 x = __ldg(pos + st + i);
-            if (lam) x.w = __ldg(lam + st + i);
-            if (vel) {
-                const float4 v = __ldg(vel + st + i);
-                x.w = v.x;
-                sv[bs + i] = make_float2(v.y, v.z);
-            }
+            x.w = __ldg(lam + st + i);
             sp[bs + i] = x;
         }
     }
+    __syncthreads();
 }
 
-// Plans the CTA's tile and stages it when it is staged and its scene has
-// lists; returns whether the tile is staged.  CTA-uniform; every thread
-// calls it.
-template <class Sh, class Scenes>
-__device__ __forceinline__ bool plan_and_stage(TilePlan& P, const uint32_t* __restrict__ key_s,
-                                               const uint32_t* __restrict__ lb, const Scenes& S,
-                                               const ListBufs& lbuf, uint32_t t0, uint32_t N,
-                                               const float4* __restrict__ pos, const float* __restrict__ lam,
-                                               const float4* __restrict__ vel, float4* sp, float2* sv) {
-    if (lbuf.cap == 0) return false;
-    if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N);
+template <class Sh>
+__device__ __forceinline__ void stage_finish(TilePlan& P, bool staged, const float* __restrict__ lam,
+                                             const float4* __restrict__ vel, float4* sp, float2* sv,
+                                             uint32_t* err) {
+    if (!staged) return;
+    if (!mbar_wait_bounded(&P.bar, 0u, kSpinLimit)) {
+        if (err) atomicOr(err, kErrStageTimeoutBit);
+        mbar_wait_bounded(&P.bar, 0u, kSpinLimit);
+    }
+    if (!lam && !vel) return;
+    for (int r = 0; r < P.nrows; ++r) {
+        const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
+        for (uint32_t i = threadIdx.x; i < len; i += Sh::kTile) {
+            float* w = reinterpret_cast<float*>(sp + bs + i) + 3;
+            if (lam) *w = __ldg(lam + st + i);
+            if (vel) {
+                const float4 v = __ldg(vel + st + i);
+                *w = v.x;
+                sv[bs + i] = make_float2(v.y, v.z);
+            }
+        }
+    }
     __syncthreads();
-    const bool staged = P.staged && P.lists && lbuf.staging;
-    if (staged) stage_tile<Sh>(P, pos, lam, vel, sp, sv);
-    __syncthreads();
-    return staged;
 }
 
 // Packed two-lane FP32 arithmetic (Blackwell f32x2): the list test of two
@@ -566,7 +601,8 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
 template <class Scenes, class Sh>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                                                  Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf) {
+                                                  Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf,
+                                                  uint32_t* __restrict__ err) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -578,9 +614,10 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_stage<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, nullptr, sp, nullptr);
+    const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
     const float4 pi = pred[sc];
     const GlobalData g{pred, nullptr, nullptr};
+    stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
     uint32_t n;
     float l = 0.f;
     if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
@@ -626,7 +663,8 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_stage<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, lam, nullptr, sp, nullptr);
+    const bool staged = plan_and_issue<Sh, false>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+    stage_rows<Sh>(P, staged, pred, lam, sp);
     const float4 pi = pred[sc];
     const float lam_i = lam[sc];
     const float w_q = scorr_wq(dp);
@@ -708,7 +746,8 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
         float4* sp = smem;
         float2* sv = reinterpret_cast<float2*>(smem + Sh::kStageMax);
         const bool xs = s < N && dp.xsph_c > 0.f;  // every lane takes part in the warp-wide rounds
-        const bool staged = plan_and_stage<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, nullptr, vel_s, sp, sv);
+        const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+        stage_finish<Sh>(P, staged, nullptr, vel_s, sp, sv, err);
         // Queue of the queued walks: the stage area, free in tiles that are
         // not staged.  In a staged tile a warp whose lists overflowed walks
         // the stencil without a queue.
@@ -1013,7 +1052,7 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
         const unsigned g = blocks_for(sh.N, Sh::kTile);
         if (which == 0)
             k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s,
-                                                                         list_bufs(b, sh));
+                                                                         list_bufs(b, sh), b.err);
         else
             k_delta<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt,
                                                                         b.pos_s, b.vel_s, list_bufs(b, sh));
@@ -1080,7 +1119,7 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
         const unsigned g = blocks_for(m.N, Sh::kTile);
         if (which == 0)
             k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N, m.lam_s,
-                                                                           lb);
+                                                                           lb, m.err);
         else
             k_delta<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N,
                                                                           nxt, m.pos_s, m.vel_s, lb);
