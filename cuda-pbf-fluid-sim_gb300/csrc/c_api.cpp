@@ -602,6 +602,17 @@ int pbf_selftest_bounded_wait(uint32_t spin_limit, void* d_scratch) {
     return (host[1] & pbf::kErrLookbackTimeoutBit) ? PBF_ERR_TIMEOUT : PBF_OK;
 }
 
+int pbf_selftest_stage_wait(uint32_t spin_limit, void* d_scratch) {
+    if (!d_scratch) return PBF_ERR_INVALID;
+    uint32_t* w = static_cast<uint32_t*>(d_scratch);
+    cudaError_t e = pbf::fused_selftest_stage_wait(spin_limit, w, 0);
+    if (e != cudaSuccess) return from_cuda(e);
+    uint32_t host = 0;
+    e = cudaMemcpy(&host, w, sizeof(host), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return from_cuda(e);
+    return (host & pbf::kErrStageTimeoutBit) ? PBF_ERR_TIMEOUT : PBF_OK;
+}
+
 // ------------------------------------------- reference-name entry points
 // Exact symbols and signatures of the reference's extern "C" launchers, so a
 // reference build can link this library instead of compiling sim/*.cu.

@@ -1141,6 +1141,26 @@ cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStrea
     });
 }
 
+// Failure path of the staging wait: one block arms its barrier for 16 bytes
+// that no copy delivers, so the bounded wait gives up, records
+// kErrStageTimeoutBit in err[0] and returns (no copy is in flight).
+__global__ void k_selftest_stage_wait(uint32_t limit, uint32_t* __restrict__ err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_arrive_expect_tx(&bar, 16u);
+    }
+    __syncthreads();
+    if (!mbar_wait_bounded(&bar, 0u, limit) && threadIdx.x == 0) atomicOr(err, kErrStageTimeoutBit);
+}
+
+cudaError_t fused_selftest_stage_wait(uint32_t spin_limit, uint32_t* d_err, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_selftest_stage_wait<<<1, 32, 0, s>>>(spin_limit, d_err);
+    return cudaGetLastError();
+}
+
 cudaError_t fused_scatter_lambda(const FusedBufs& b, const FusedShape& sh, float* lambda_by_id, cudaStream_t s) {
     if (sh.N == 0) return cudaSuccess;
     k_scatter_lambda<<<blocks_for(sh.N, kBS), kBS, 0, s>>>(b.lam_s, b.perm, sh.N, lambda_by_id);

@@ -149,6 +149,10 @@ cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStrea
 // as scratch).  Writes 4 doubles to b.stats_out.
 cudaError_t fused_density_stats(const FusedBufs& b, const FusedShape& sh, cudaStream_t s);
 
+// Failure-path self-test of the staging barrier's bounded wait (see
+// pbf_selftest_stage_wait); d_err receives the error word.
+cudaError_t fused_selftest_stage_wait(uint32_t spin_limit, uint32_t* d_err, cudaStream_t s);
+
 // lambda (by original id) of the last iteration, for inspection.
 cudaError_t fused_scatter_lambda(const FusedBufs& b, const FusedShape& sh, float* lambda_by_id, cudaStream_t s);
 

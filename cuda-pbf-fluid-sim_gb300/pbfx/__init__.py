@@ -146,6 +146,7 @@ _SIGS = {
     "pbf_density_stats": ([_VP, C.POINTER(C.c_double * 4)], _I),
     "pbf_debug_fetch": ([_VP, _I, _VP, _SZ], _I),
     "pbf_selftest_bounded_wait": ([_U32, _VP], _I),
+    "pbf_selftest_stage_wait": ([_U32, _VP], _I),
     "pbf_selftest_powf4": ([C.POINTER(C.c_uint64), C.POINTER(_U32)], _I),
     "pbf_debug_eval_math": ([_I, _VP, _VP, _VP, _U32], _I),
     "pbf_profile_step": ([_VP, C.POINTER(SimParams), C.POINTER(C.c_float), C.POINTER(C.c_char_p), _I,

@@ -371,6 +371,13 @@ int pbf_selftest_powf4(uint64_t* mismatches, uint32_t* first_mismatch_bits);
  * Returns PBF_ERR_TIMEOUT when the wait gave up as designed. */
 int pbf_selftest_bounded_wait(uint32_t spin_limit, void* d_scratch);
 
+/* The same for the wait on a tile's shared-memory staging (TMA bulk copies
+ * completing on an mbarrier): one block arms its barrier for bytes that no
+ * copy delivers; after spin_limit polls it records the stage timeout and
+ * returns.  d_scratch: caller-owned device memory of >= 4 bytes.  Returns
+ * PBF_ERR_TIMEOUT when the wait gave up as designed. */
+int pbf_selftest_stage_wait(uint32_t spin_limit, void* d_scratch);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

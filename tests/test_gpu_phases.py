@@ -312,6 +312,16 @@ def test_bounded_wait_gives_up_and_context_survives(gpu, lib):
     assert x == 45
 
 
+def test_stage_wait_gives_up_and_context_survives(gpu, lib):
+    """The staging barrier's wait (TMA bulk copies into shared memory) is
+    bounded: armed for bytes that never arrive, it records the timeout."""
+    torch = gpu
+    scratch = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert lib.pbf_selftest_stage_wait(2000, P(scratch)) == pbfx.PBF_ERR_TIMEOUT
+    x = torch.arange(10, device="cuda").sum().item()
+    assert x == 45
+
+
 def test_scorr_exponent_four_matches_runtime_powf_everywhere(gpu, lib):
     """The delta kernels' s_corr exponent n == 4 form equals powf(x, n) with n
     known only at run time, for every non-negative float (2.1e9 values)."""
