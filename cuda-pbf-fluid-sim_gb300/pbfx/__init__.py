@@ -170,6 +170,16 @@ _SIGS = {
     "pbf_ensemble_synchronize": ([_VP], _I),
     "pbf_ensemble_launches_per_step": ([_VP], _I),
     "pbf_neighbour_list_stats": ([_VP, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32), _I], _I),
+    "pbf_console_create": ([C.POINTER(_VP)], _I),
+    "pbf_console_destroy": ([_VP], _I),
+    "pbf_console_set": ([_VP, C.c_char_p, C.c_double], _I),
+    "pbf_console_get": ([_VP, C.c_char_p, C.POINTER(C.c_double)], _I),
+    "pbf_console_prepare_cube_mix": ([_VP], _I),
+    "pbf_console_merge_json": ([_VP, C.c_char_p, C.c_char_p, _U32], _I),
+    "pbf_console_profile": ([_VP, C.c_char_p, _U32], _I),
+    "pbf_console_build_sim_params": ([_VP, _I, C.POINTER(SimParams)], _I),
+    "pbf_console_cube_mix_centers": ([_VP, C.POINTER(_F), _U32, C.POINTER(_U32)], _I),
+    "pbf_seed_cube_mix": ([_VP, _VP], _I),
     "pbf_tile_shape_count": ([], _I),
     "pbf_tile_shape_info": ([_I, C.POINTER(_I), C.POINTER(_I)], _I),
     "pbf_set_tile_shape": ([_VP, _I], _I),
@@ -465,6 +475,64 @@ class Ensemble:
         chosen = _I()
         check(self.lib.pbf_ensemble_autotune(self.h, steps, ms, C.byref(chosen)), "ensemble autotune")
         return int(chosen.value), [float(x) for x in ms]
+
+
+class Console:
+    """Owning wrapper of a pbf_console: the reference application's runtime
+    configuration (RuntimeConsole) and its mapping to SimParams.  Fields are
+    read and written by name, e.g. con["sim.particleRadiusWorld"] = 0.005."""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self.h = _VP()
+        check(lib.pbf_console_create(C.byref(self.h)), "console_create")
+
+    def close(self):
+        if self.h:
+            self.lib.pbf_console_destroy(self.h)
+            self.h = _VP()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __getitem__(self, field: str) -> float:
+        v = C.c_double()
+        check(self.lib.pbf_console_get(self.h, field.encode(), C.byref(v)), "console_get " + field)
+        return float(v.value)
+
+    def __setitem__(self, field: str, value: float):
+        check(self.lib.pbf_console_set(self.h, field.encode(), float(value)), "console_set " + field)
+
+    def prepare_cube_mix(self):
+        check(self.lib.pbf_console_prepare_cube_mix(self.h), "console_prepare_cube_mix")
+
+    def merge_json(self, text: str):
+        """Merges a config.json text; raises ValueError (console unchanged) if it is rejected."""
+        err = C.create_string_buffer(512)
+        if self.lib.pbf_console_merge_json(self.h, text.encode(), err, len(err)) != PBF_OK:
+            raise ValueError(err.value.decode())
+
+    def profile(self) -> str:
+        buf = C.create_string_buffer(256)
+        check(self.lib.pbf_console_profile(self.h, buf, len(buf)), "console_profile")
+        return buf.value.decode()
+
+    def sim_params(self, sanitize: bool = True) -> SimParams:
+        p = SimParams()
+        check(self.lib.pbf_console_build_sim_params(self.h, int(sanitize), C.byref(p)), "console_build_sim_params")
+        return p
+
+    def cube_mix_centers(self) -> np.ndarray:
+        n = _U32()
+        check(self.lib.pbf_console_cube_mix_centers(self.h, None, 0, C.byref(n)), "console_cube_mix_centers")
+        out = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            check(self.lib.pbf_console_cube_mix_centers(self.h, out.ctypes.data_as(C.POINTER(_F)), n.value,
+                                                        C.byref(n)), "console_cube_mix_centers")
+        return out
 
 
 def tile_shapes(lib):

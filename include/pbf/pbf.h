@@ -364,6 +364,44 @@ int pbf_debug_eval_math(int fn, const float* d_a, const float* d_b, float* d_out
  * 0xFFFFFFFF if none. */
 int pbf_selftest_powf4(uint64_t* mismatches, uint32_t* first_mismatch_bits);
 
+/* Runtime configuration (headless console::RuntimeConsole, include/pbf/console.h):
+ * the reference application's defaults, CubeMix scene derivation, config.json
+ * merge and RuntimeConsole -> SimParams mapping.  A console is a host object;
+ * none of these calls touch the GPU except pbf_seed_cube_mix. */
+typedef struct pbf_console pbf_console;
+/* Defaults of the reference's RuntimeConsole, CubeMix derived (numParticles,
+ * simulation box). */
+int pbf_console_create(pbf_console** out);
+int pbf_console_destroy(pbf_console* c);
+/* Fields by name: "sim.<field>", "sim.pbf.<field>", "sim.gravity.x",
+ * "sim.gridMins.y", "perf.<field>" (RuntimeConsole names).  Booleans read and
+ * write 0 / 1, sim.massMode 0 (explicit), 1 (sphere by radius), 2 (uniform
+ * lattice).  PBF_ERR_INVALID for an unknown name or an out-of-range value.
+ * Setting CubeMix fields does not re-derive the scene: call
+ * pbf_console_prepare_cube_mix. */
+int pbf_console_set(pbf_console* c, const char* field, double value);
+int pbf_console_get(pbf_console* c, const char* field, double* value);
+int pbf_console_prepare_cube_mix(pbf_console* c);
+/* Merges a config.json text ("performance", "simulation", "profile",
+ * "profiles"; other sections are application state and are ignored), then
+ * re-derives the CubeMix scene.  PBF_ERR_INVALID, the console unchanged and a
+ * message in err (err_cap bytes, may be NULL) when the text is not JSON or a
+ * known key has a value of the wrong type. */
+int pbf_console_merge_json(pbf_console* c, const char* text, char* err, uint32_t err_cap);
+/* Name of the active profile ("" if none); PBF_ERR_INVALID if cap is too small. */
+int pbf_console_profile(pbf_console* c, char* name, uint32_t cap);
+/* BuildSimParams of the reference (then, with sanitize != 0, the
+ * application's clamps: solverIters [1, 64], maxNeighbors [8, neighbor cap or
+ * 1024], sortEveryN >= 1), starting from a value-initialised SimParams. */
+int pbf_console_build_sim_params(pbf_console* c, int sanitize, pbf_sim_params* out);
+/* CubeMix group centres (x, y, z per group); xyz may be NULL to query *count. */
+int pbf_console_cube_mix_centers(pbf_console* c, float* xyz, uint32_t cap, uint32_t* count);
+/* Seeds the simulation's particles as the reference application does for the
+ * CubeMix scene: cubes of cube_edge_particles^3 at the group centres, lattice
+ * spacing h * cube_lattice_spacing_factor_h, seeded jitter.  The simulation's
+ * particle count must equal the scene's. */
+int pbf_seed_cube_mix(pbf_sim* sim, pbf_console* c);
+
 /* Failure-path self-test of the bounded device waits: one block polls a
  * look-back status that nothing ever publishes.  After spin_limit polls the
  * kernel records the timeout in its error word and returns, leaving the
