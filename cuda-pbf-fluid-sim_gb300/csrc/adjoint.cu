@@ -200,7 +200,8 @@ __global__ void __launch_bounds__(kBS) k_adj_velocity(const float4* __restrict__
 // ----------------------------------------------------------------- delta
 // x^{k+1}_i = x^k_i + clampDisp(relax / rho0 * sum_j (l_i + l_j + scorr_ij) a_ij)
 __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__ x, const float* __restrict__ lam,
-                                                      Cand cand, const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                      const float4* __restrict__ dsum, Cand cand,
+                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                       const float4* __restrict__ xbar_in,
                                                       float4* __restrict__ xbar_out, float* __restrict__ lambar) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -211,16 +212,8 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
     const float li = lam[s];
     const float w_q = scorr_wq(dp);
     const float3 gin = f3(xbar_in[s]);
-    // forward displacement, for the clamp
-    float3 D = make_float3(0.f, 0.f, 0.f);
-    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
-        if (k == s) return true;
-        float rx, ry, rz;
-        const float r2 = dist2(xi, x[k], rx, ry, rz);
-        if (r2 > dp.kernel.h2) return true;
-        delta_accumulate(D, rx, ry, rz, r2, li, lam[k], w_q, dp);
-        return true;
-    });
+    // forward displacement before the clamp, as the replay recorded it
+    const float3 D = f3(dsum[s]);
     const float invRest = (dp.restDensity > 0.f) ? 1.0f / dp.restDensity : 0.f;
     const float omega = pbf.enable_relax ? pbf.relax_omega : 1.0f;
     const float3 d = make_float3(D.x * invRest * omega, D.y * invRest * omega, D.z * invRest * omega);
@@ -249,11 +242,22 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
             const float hr2 = dp.kernel.h2 - q.r2;
             const float w = dp.kernel.poly6 * hr2 * hr2 * hr2;
             const float ratio = (w_q > 0.f) ? w / w_q : 0.f;
-            scorr = -kcorr * powf(ratio, ncorr);
+            // ratio^n and ratio^(n-1); products for the default n = 4 (the
+            // adjoint is FP32 calculus, not a replay of the forward's bits)
+            float rn, rn1;
+            if (ncorr == 4.0f) {
+                const float q2 = ratio * ratio;
+                rn1 = q2 * ratio;
+                rn = q2 * q2;
+            } else {
+                rn = powf(ratio, ncorr);
+                rn1 = powf(ratio, ncorr - 1.0f);
+            }
+            scorr = -kcorr * rn;
             const bool floored = pbf.scorr_min < 0.f && scorr < pbf.scorr_min;
             if (floored) scorr = pbf.scorr_min;
             if (!floored && w_q > 0.f && ratio > 0.f)
-                dscorr = -kcorr * ncorr * powf(ratio, ncorr - 1.0f) * (-3.0f * dp.kernel.poly6 * hr2 * hr2) / w_q;
+                dscorr = -kcorr * ncorr * rn1 * (-3.0f * dp.kernel.poly6 * hr2 * hr2) / w_q;
         }
         const float lij = li + lam[k] + scorr;
         const float lbar = dot3(Db, a);
@@ -489,6 +493,7 @@ GridDesc grid_desc(const sim::GridBounds& g, int res) {
 struct StepRecord {
     std::vector<float4*> x;  // x[0..iters]: predictions of each iteration; x[iters] = solved (clamped)
     std::vector<float*> lam;  // lambda of each iteration
+    std::vector<float4*> D;   // delta's neighbour sum of each iteration (before the clamp)
     float4* vf = nullptr;     // velocity before XSPH
     float4* ps = nullptr;     // step-start positions
     uint32_t* key_s = nullptr;
@@ -591,6 +596,7 @@ struct pbf_tape {
             bi.pred_a = (it % 2 == 0) ? cur : nxt;
             bi.pred_b = (it % 2 == 0) ? nxt : cur;
             bi.lam_s = r.lam[it];
+            bi.delta_sum = r.D[it];
             if ((e = fused_solve_phase(bi, sh, it, 0, stream)) != cudaSuccess) return e;
             if ((e = fused_solve_phase(bi, sh, it, 1, stream)) != cudaSuccess) return e;
         }
@@ -619,7 +625,7 @@ struct pbf_tape {
         for (int it = iters - 1; it >= 0; --it) {
             cudaMemsetAsync(xout, 0, b4, stream);
             cudaMemsetAsync(lambar, 0, sizeof(float) * N, stream);
-            k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], cand, dp, N, xin, xout, lambar);
+            k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], r.D[it], cand, dp, N, xin, xout, lambar);
             k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], cand, dp, N, lambar, xout);
             std::swap(xin, xout);
         }
@@ -676,8 +682,10 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
         if (!ok) break;
         r.x.assign(size_t(std::max(t->iters, 0) + 1), nullptr);
         r.lam.assign(size_t(std::max(t->iters, 0)), nullptr);
+        r.D.assign(size_t(std::max(t->iters, 0)), nullptr);
         for (auto& x : r.x) ok = ok && t->alloc(&x, N);
         for (auto& l : r.lam) ok = ok && t->alloc(&l, N);
+        for (auto& dd : r.D) ok = ok && t->alloc(&dd, N);
         ok = ok && t->alloc(&r.vf, N) && t->alloc(&r.ps, N) && t->alloc(&r.key_s, N) && t->alloc(&r.perm, N) &&
              t->alloc(&r.lb, size_t(t->numCells) + 1);
         if (ok && t->listCap) ok = t->alloc(&r.list, size_t(N) * t->listCap) && t->alloc(&r.count, N);

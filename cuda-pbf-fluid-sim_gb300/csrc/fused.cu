@@ -651,7 +651,8 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
                                                  const float* __restrict__ lam, const uint32_t* __restrict__ key_s,
                                                  const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
                                                  float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
-                                                 float4* __restrict__ vel_s, ListBufs lbuf) {
+                                                 float4* __restrict__ vel_s, ListBufs lbuf,
+                                                 float4* __restrict__ dsum_out) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -674,25 +675,29 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
     if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            d = delta_queued<kQueue, Sh::kTile>(active, sc, pi, lam_i,
+            d = delta_queued_sum<kQueue, Sh::kTile>(active, sc, pi, lam_i,
                                             ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                             w_q, StagedData{sp, nullptr}, q16);
         else
-            d = delta_queued<kQueue, Sh::kTile>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
+            d = delta_queued_sum<kQueue, Sh::kTile>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
                                             q32);
     } else if (staged) {
         int cx, cy, cz;
         decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            d = delta_of(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb + v.cellOffset},
+            d = delta_of_sum(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb + v.cellOffset},
                          [&](uint32_t k, uint32_t& j, float& lj) {
                              j = k;
                              lj = __ldg(lam + k);
                              return __ldg(pred + k);
                          });
     } else {
-        d = delta_queued<kQueue, Sh::kTile>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
+        d = delta_queued_sum<kQueue, Sh::kTile>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
     }
+    // the neighbour sum, for the adjoint's replay (which needs the displacement
+    // before the clamp)
+    if (dsum_out && active) dsum_out[s] = make_float4(d.x, d.y, d.z, 0.f);
+    if (active) d = delta_finalize(d, dp);
     if (s >= N) return;
     const bool last = active ? it == v.iters - 1 : (v.iters <= 0 && it == 0);
     float4 x = active ? make_float4(add_(pi.x, d.x), add_(pi.y, d.y), add_(pi.z, d.z), pi.w) : pi;
@@ -1055,7 +1060,8 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
                                                                          list_bufs(b, sh), b.err);
         else
             k_delta<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt,
-                                                                        b.pos_s, b.vel_s, list_bufs(b, sh));
+                                                                        b.pos_s, b.vel_s, list_bufs(b, sh),
+                                                                        b.delta_sum);
         return cudaGetLastError();
     });
 }
@@ -1122,7 +1128,7 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
                                                                            lb, m.err);
         else
             k_delta<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N,
-                                                                          nxt, m.pos_s, m.vel_s, lb);
+                                                                          nxt, m.pos_s, m.vel_s, lb, nullptr);
         return cudaGetLastError();
     });
 }

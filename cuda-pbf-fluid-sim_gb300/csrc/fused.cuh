@@ -29,6 +29,9 @@ struct FusedBufs {
     uint32_t* perm;
     float4* pred_a;
     float4* pred_b;
+    // Optional (null: not written): the delta pass's neighbour sum per sorted
+    // slot, before the displacement clamp (the adjoint's replay records it).
+    float4* delta_sum;
     float4* pos_s;
     float4* vel_s;
     float* lam_s;

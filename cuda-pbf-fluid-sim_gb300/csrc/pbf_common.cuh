@@ -691,9 +691,9 @@ __device__ __forceinline__ float3 delta_finalize(float3 dsum, const sim::DeviceP
 }
 
 // fetch(k, j, lam_j) returns the candidate position and writes its identity
-// and lambda.
+// and lambda.  *_sum: the neighbour sum before delta_finalize.
 template <class RowRange, class Fetch>
-__device__ __forceinline__ float3 delta_of(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
+__device__ __forceinline__ float3 delta_of_sum(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
                                            const sim::DeviceParams& dp, float w_q, RowRange&& rows, Fetch&& fetch) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
     walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
@@ -707,11 +707,17 @@ __device__ __forceinline__ float3 delta_of(uint32_t self, float4 pi, float lam_i
         delta_accumulate(dsum, rx, ry, rz, r2, lam_i, lam_j, w_q, dp);
         return true;
     });
-    return delta_finalize(dsum, dp);
+    return dsum;
+}
+
+template <class RowRange, class Fetch>
+__device__ __forceinline__ float3 delta_of(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
+                                           const sim::DeviceParams& dp, float w_q, RowRange&& rows, Fetch&& fetch) {
+    return delta_finalize(delta_of_sum(self, pi, lam_i, cx, cy, cz, dp, w_q, rows, fetch), dp);
 }
 
 template <int Q, int kStride, class Src, class Data, class QT>
-__device__ __forceinline__ float3 delta_queued(bool active, uint32_t s, float4 pi, float lam_i, const Src& src,
+__device__ __forceinline__ float3 delta_queued_sum(bool active, uint32_t s, float4 pi, float lam_i, const Src& src,
                                                const sim::DeviceParams& dp, float w_q, const Data& data, QT* q) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
     const float h2 = dp.kernel.h2;
@@ -728,7 +734,7 @@ __device__ __forceinline__ float3 delta_queued(bool active, uint32_t s, float4 p
             const float r2 = dist2(pi, pj, rx, ry, rz);
             delta_accumulate(dsum, rx, ry, rz, r2, lam_i, data.l(k, pj), w_q, dp);
         });
-    return delta_finalize(dsum, dp);
+    return dsum;
 }
 
 // ------------------------------------------------------------------ xsph
