@@ -280,7 +280,8 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
 
 // ---------------------------------------------------------------- lambda
 // lambda_i = -(rho_i / rho0 - 1) / (scale^2 (sum_j |a_ij|^2 + |sum_j a_ij|^2) + eps)
-__global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict__ x, Cand cand,
+__global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict__ x,
+                                                       const float4* __restrict__ accs, Cand cand,
                                                        const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                        const float* __restrict__ lambar,
                                                        float4* __restrict__ xbar_out) {
@@ -292,16 +293,17 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict_
     if (lb_i == 0.f) return;
     const float4 xi = x[s];
     const int cap = dp.maxNeighbors > 0 ? dp.maxNeighbors : 0x7FFFFFFF;
+    // the forward's neighbour sums, as the replay recorded them
     LambdaAcc acc;
-    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
-        if (acc.contrib >= cap) return false;
-        if (k == s) return true;
-        float rx, ry, rz;
-        const float r2 = dist2(xi, x[k], rx, ry, rz);
-        if (r2 > dp.kernel.h2) return true;
-        lambda_accumulate(acc, rx, ry, rz, r2, dp);
-        return true;
-    });
+    {
+        const float4 a0 = accs[2 * size_t(s)], a1 = accs[2 * size_t(s) + 1];
+        acc.density = a0.x;
+        acc.sumGrad2 = a0.y;
+        acc.gx = a0.z;
+        acc.gy = a0.w;
+        acc.gz = a1.x;
+        acc.contrib = int(a1.y);
+    }
     // the forward's branches (lambda_finalize)
     const float rho0 = dp.restDensity;
     const float scale = (rho0 > 0.f) ? dp.particleMass / rho0 : 0.f;
@@ -494,6 +496,7 @@ struct StepRecord {
     std::vector<float4*> x;  // x[0..iters]: predictions of each iteration; x[iters] = solved (clamped)
     std::vector<float*> lam;  // lambda of each iteration
     std::vector<float4*> D;   // delta's neighbour sum of each iteration (before the clamp)
+    std::vector<float4*> A;   // lambda's neighbour sums of each iteration (2 float4 per particle)
     float4* vf = nullptr;     // velocity before XSPH
     float4* ps = nullptr;     // step-start positions
     uint32_t* key_s = nullptr;
@@ -597,6 +600,7 @@ struct pbf_tape {
             bi.pred_b = (it % 2 == 0) ? nxt : cur;
             bi.lam_s = r.lam[it];
             bi.delta_sum = r.D[it];
+            bi.lambda_acc = r.A[it];
             if ((e = fused_solve_phase(bi, sh, it, 0, stream)) != cudaSuccess) return e;
             if ((e = fused_solve_phase(bi, sh, it, 1, stream)) != cudaSuccess) return e;
         }
@@ -626,7 +630,7 @@ struct pbf_tape {
             cudaMemsetAsync(xout, 0, b4, stream);
             cudaMemsetAsync(lambar, 0, sizeof(float) * N, stream);
             k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], r.D[it], cand, dp, N, xin, xout, lambar);
-            k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], cand, dp, N, lambar, xout);
+            k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.A[it], cand, dp, N, lambar, xout);
             std::swap(xin, xout);
         }
         k_adj_predict<<<g, kBS, 0, stream>>>(r.x[0], xin, pbar_s, r.perm, dp, N, pbar, vbar);
@@ -683,9 +687,11 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
         r.x.assign(size_t(std::max(t->iters, 0) + 1), nullptr);
         r.lam.assign(size_t(std::max(t->iters, 0)), nullptr);
         r.D.assign(size_t(std::max(t->iters, 0)), nullptr);
+        r.A.assign(size_t(std::max(t->iters, 0)), nullptr);
         for (auto& x : r.x) ok = ok && t->alloc(&x, N);
         for (auto& l : r.lam) ok = ok && t->alloc(&l, N);
         for (auto& dd : r.D) ok = ok && t->alloc(&dd, N);
+        for (auto& aa : r.A) ok = ok && t->alloc(&aa, 2 * size_t(N));
         ok = ok && t->alloc(&r.vf, N) && t->alloc(&r.ps, N) && t->alloc(&r.key_s, N) && t->alloc(&r.perm, N) &&
              t->alloc(&r.lb, size_t(t->numCells) + 1);
         if (ok && t->listCap) ok = t->alloc(&r.list, size_t(N) * t->listCap) && t->alloc(&r.count, N);

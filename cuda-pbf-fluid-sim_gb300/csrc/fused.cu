@@ -602,7 +602,7 @@ template <class Scenes, class Sh>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf,
-                                                  uint32_t* __restrict__ err) {
+                                                  uint32_t* __restrict__ err, float4* __restrict__ acc_out) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -619,27 +619,33 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     const GlobalData g{pred, nullptr, nullptr};
     stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
     uint32_t n;
-    float l = 0.f;
+    LambdaAcc a;
     if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            l = lambda_queued<kQueue, Sh::kTile>(active, sc, pi,
+            a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
                                              ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                              StagedData{sp, nullptr}, q16);
         else
-            l = lambda_queued<kQueue, Sh::kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
+            a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
     } else if (staged) {
         int cx, cy, cz;
         decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            l = lambda_of(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
+            a = lambda_of_acc(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
                 j = k;
                 return __ldg(pred + k);
             });
     } else {
-        l = lambda_queued<kQueue, Sh::kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
+        a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
     }
-    if (active) lam[s] = l;
+    if (!active) return;
+    // the neighbour sums, for the adjoint's replay
+    if (acc_out) {
+        acc_out[2 * size_t(s)] = make_float4(a.density, a.sumGrad2, a.gx, a.gy);
+        acc_out[2 * size_t(s) + 1] = make_float4(a.gz, float(a.contrib), 0.f, 0.f);
+    }
+    lam[s] = lambda_finalize(a, dp);
 }
 
 // delta of iteration `it`.  The scene's last iteration also applies the
@@ -1057,7 +1063,7 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
         const unsigned g = blocks_for(sh.N, Sh::kTile);
         if (which == 0)
             k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s,
-                                                                         list_bufs(b, sh), b.err);
+                                                                         list_bufs(b, sh), b.err, b.lambda_acc);
         else
             k_delta<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt,
                                                                         b.pos_s, b.vel_s, list_bufs(b, sh),
@@ -1125,7 +1131,7 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
         const unsigned g = blocks_for(m.N, Sh::kTile);
         if (which == 0)
             k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N, m.lam_s,
-                                                                           lb, m.err);
+                                                                           lb, m.err, nullptr);
         else
             k_delta<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N,
                                                                           nxt, m.pos_s, m.vel_s, lb, nullptr);

@@ -32,6 +32,9 @@ struct FusedBufs {
     // Optional (null: not written): the delta pass's neighbour sum per sorted
     // slot, before the displacement clamp (the adjoint's replay records it).
     float4* delta_sum;
+    // Optional: the lambda pass's neighbour sums per sorted slot, two float4
+    // each: (density, sum |grad|^2, grad x, grad y), (grad z, contributions).
+    float4* lambda_acc;
     float4* pos_s;
     float4* vel_s;
     float* lam_s;

@@ -570,9 +570,10 @@ __device__ __forceinline__ float lambda_finalize(const LambdaAcc& a, const sim::
 }
 
 // Single-pass walk (reference layout): fetch(k, j) returns the candidate's
-// position and writes its identity j (compared with `self`).
+// position and writes its identity j (compared with `self`).  *_acc: the
+// neighbour sums before lambda_finalize.
 template <class RowRange, class Fetch>
-__device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int cy, int cz,
+__device__ __forceinline__ LambdaAcc lambda_of_acc(uint32_t self, float4 pi, int cx, int cy, int cz,
                                            const sim::DeviceParams& dp, RowRange&& rows, Fetch&& fetch) {
     LambdaAcc a;
     const int cap = dp.maxNeighbors;
@@ -588,7 +589,13 @@ __device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int
         lambda_accumulate(a, rx, ry, rz, r2, dp);
         return true;
     });
-    return lambda_finalize(a, dp);
+    return a;
+}
+
+template <class RowRange, class Fetch>
+__device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int cy, int cz,
+                                           const sim::DeviceParams& dp, RowRange&& rows, Fetch&& fetch) {
+    return lambda_finalize(lambda_of_acc(self, pi, cx, cy, cz, dp, rows, fetch), dp);
 }
 
 // Two-phase walk over cell-ordered positions (slot k is particle k); Src is
@@ -596,7 +603,7 @@ __device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int
 // Stencil candidates include the particle itself (rejected by slot); lists
 // never do.
 template <int Q, int kStride, class Src, class Data, class QT>
-__device__ __forceinline__ float lambda_queued(bool active, uint32_t s, float4 pi, const Src& src,
+__device__ __forceinline__ LambdaAcc lambda_queued_acc(bool active, uint32_t s, float4 pi, const Src& src,
                                                const sim::DeviceParams& dp, const Data& data, QT* q) {
     LambdaAcc a;
     const int cap = dp.maxNeighbors;
@@ -613,7 +620,7 @@ __device__ __forceinline__ float lambda_queued(bool active, uint32_t s, float4 p
             const float r2 = dist2(pi, data.p(k), rx, ry, rz);
             lambda_accumulate(a, rx, ry, rz, r2, dp);
         });
-    return lambda_finalize(a, dp);
+    return a;
 }
 
 // s_corr exponent: powf, as the reference (sim/pbf_delta_apply.cu:82).
