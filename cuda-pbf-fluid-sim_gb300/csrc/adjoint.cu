@@ -16,9 +16,14 @@
 // order).  Clamps contribute the derivative of the branch taken: a clamped
 // position axis, a clamped lambda, a lambda zeroed for too few neighbours and
 // an s_corr held at its floor pass no gradient; the displacement clamp passes
-// the Jacobian of d * maxDisp / |d|.  Every particle gathers its own terms;
-// terms that belong to a neighbour are added to it with float atomics, so
-// gradients agree run to run only to rounding.
+// the Jacobian of d * maxDisp / |d|.  A pair's terms are symmetric (a_ji =
+// -a_ij, the same weights and Jacobian), so every particle gathers both the
+// terms of its own equation and those its neighbours' equations hold for it,
+// from small per-particle arrays (the clamp-projected gradient of delta, the
+// coefficients of lambda and the slot of each particle's last counted
+// neighbour): no atomics, and the gradients are the same bits run to run.
+// (With the XSPH gate on, each particle's XSPH weight depends on its
+// neighbour count; that case scatters with float atomics.)
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -171,6 +176,83 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ 
     if (threadIdx.x == 0 && cbar) atomicAdd(cbar, red[0]);
 }
 
+// Gathered XSPH adjoint (gate off: the weight c (m / rho0) is the same for
+// every particle).  Particle j collects
+//   dL/dv_j = g_j (1 - c sum_k W_jk) + c sum_k W_jk g_k,
+//   dL/dx_j += sum_k 2 (x_j - x_k) c W'(r2) (v_k - v_j) . (g_j - g_k),
+// with W'(r2) = -3 poly6 (h^2 - r2)^2, and its part of dL/dc in a per-block
+// partial (summed in a fixed order by k_sum_partials).
+__global__ void __launch_bounds__(kAdjBS) k_adj_xsph_gather(const float4* __restrict__ xf,
+                                                            const float4* __restrict__ vf, Cand cand,
+                                                            const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                            const float4* __restrict__ vbar_out,
+                                                            float4* __restrict__ vfbar, float4* __restrict__ xfbar,
+                                                            float* __restrict__ cpart_blocks) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    float cpart = 0.f;
+    if (s < N) {
+        const sim::DeviceParams& dp = *dpp;
+        const float4 xi = xf[s], vi = vf[s];
+        const float3 g = f3(vbar_out[s]);
+        const float mor = (dp.restDensity > 0.f) ? dp.particleMass / dp.restDensity : 0.f;
+        const float ceff = dp.xsph_c * mor;
+        float wsum = 0.f;
+        float3 sum = make_float3(0.f, 0.f, 0.f), gsum = make_float3(0.f, 0.f, 0.f), xb = make_float3(0.f, 0.f, 0.f);
+        for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
+            if (k == s) return true;
+            float rx, ry, rz;
+            const float r2 = dist2(xi, xf[k], rx, ry, rz);
+            if (r2 > dp.kernel.h2) return true;
+            const float hr2 = sub_(dp.kernel.h2, r2);
+            const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
+            const float4 vj = vf[k];
+            const float3 gk = f3(vbar_out[k]);
+            const float3 dv = make_float3(vj.x - vi.x, vj.y - vi.y, vj.z - vi.z);
+            sum.x += dv.x * w;
+            sum.y += dv.y * w;
+            sum.z += dv.z * w;
+            wsum += w;
+            gsum.x += gk.x * w;
+            gsum.y += gk.y * w;
+            gsum.z += gk.z * w;
+            const float3 dg = make_float3(g.x - gk.x, g.y - gk.y, g.z - gk.z);
+            const float r2bar = ceff * dot3(dv, dg) * (-3.0f * dp.kernel.poly6 * hr2 * hr2);
+            xb.x += 2.f * rx * r2bar;
+            xb.y += 2.f * ry * r2bar;
+            xb.z += 2.f * rz * r2bar;
+            return true;
+        });
+        cpart = mor * dot3(sum, g);
+        vfbar[s] = make_float4(g.x - ceff * wsum * g.x + ceff * gsum.x, g.y - ceff * wsum * g.y + ceff * gsum.y,
+                               g.z - ceff * wsum * g.z + ceff * gsum.z, 0.f);
+        const float4 x0 = xfbar[s];
+        xfbar[s] = make_float4(x0.x + xb.x, x0.y + xb.y, x0.z + xb.z, 0.f);
+    }
+    __shared__ float red[kAdjBS];
+    red[threadIdx.x] = cpart;
+    __syncthreads();
+    for (int w = kAdjBS / 2; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cpart_blocks[blockIdx.x] = red[0];
+}
+
+// *out += the sum of n partials, in a fixed order (one block).
+__global__ void __launch_bounds__(256) k_sum_partials(const float* __restrict__ part, uint32_t n,
+                                                      float* __restrict__ out) {
+    __shared__ float red[256];
+    float v = 0.f;
+    for (uint32_t i = threadIdx.x; i < n; i += 256) v += part[i];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out += red[0];
+}
+
 // v_f = (x_f - p) / dt; x_f = clamp(x_iters).  Writes dL/dx_iters and
 // dL/dp (sorted).
 __global__ void __launch_bounds__(kBS) k_adj_velocity(const float4* __restrict__ xf,
@@ -199,21 +281,18 @@ __global__ void __launch_bounds__(kBS) k_adj_velocity(const float4* __restrict__
 
 // ----------------------------------------------------------------- delta
 // x^{k+1}_i = x^k_i + clampDisp(relax / rho0 * sum_j (l_i + l_j + scorr_ij) a_ij)
-__global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__ x, const float* __restrict__ lam,
-                                                      const float4* __restrict__ dsum, Cand cand,
-                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+// First, per particle: Db_i = (relax / rho0) J_clamp^T dL/dx^{k+1}_i, J_clamp
+// the Jacobian of the displacement clamp at the recorded pre-clamp sum.
+__global__ void __launch_bounds__(kBS) k_adj_delta_db(const float4* __restrict__ dsum,
                                                       const float4* __restrict__ xbar_in,
-                                                      float4* __restrict__ xbar_out, float* __restrict__ lambar) {
+                                                      const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                      float4* __restrict__ Db) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const sim::DeviceParams& dp = *dpp;
     const sim::PbfTuning& pbf = dp.pbf;
-    const float4 xi = x[s];
-    const float li = lam[s];
-    const float w_q = scorr_wq(dp);
-    const float3 gin = f3(xbar_in[s]);
-    // forward displacement before the clamp, as the replay recorded it
     const float3 D = f3(dsum[s]);
+    const float3 gin = f3(xbar_in[s]);
     const float invRest = (dp.restDensity > 0.f) ? 1.0f / dp.restDensity : 0.f;
     const float omega = pbf.enable_relax ? pbf.relax_omega : 1.0f;
     const float3 d = make_float3(D.x * invRest * omega, D.y * invRest * omega, D.z * invRest * omega);
@@ -228,9 +307,31 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
             db = make_float3(sc * (gin.x - d.x * proj), sc * (gin.y - d.y * proj), sc * (gin.z - d.z * proj));
         }
     }
-    const float3 Db = make_float3(db.x * invRest * omega, db.y * invRest * omega, db.z * invRest * omega);
+    Db[s] = make_float4(db.x * invRest * omega, db.y * invRest * omega, db.z * invRest * omega, 0.f);
+}
+
+// Then each particle j gathers over its neighbours k, with dDb = Db_j - Db_k:
+//   dL/dl_j = sum_k dDb . a_jk,
+//   dL/dx^k_j = dL/dx^{k+1}_j + sum_k [J_jk^T (l_jk dDb) + 2 u_jk (dDb . a_jk) dscorr/dr2],
+// both equations' terms of the pair at once (a_kj = -a_jk, the same l, s_corr
+// and Jacobian).
+__global__ void __launch_bounds__(kAdjBS) k_adj_delta_gather(const float4* __restrict__ x,
+                                                             const float* __restrict__ lam,
+                                                             const float4* __restrict__ Db, Cand cand,
+                                                             const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                             const float4* __restrict__ xbar_in,
+                                                             float4* __restrict__ xbar_out,
+                                                             float* __restrict__ lambar) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const sim::PbfTuning& pbf = dp.pbf;
+    const float4 xi = x[s];
+    const float li = lam[s];
+    const float w_q = scorr_wq(dp);
+    const float3 Dbi = f3(Db[s]);
     float lown = 0.f;
-    float3 own = gin;  // identity path x^k -> x^{k+1}
+    float3 own = f3(xbar_in[s]);  // identity path x^k -> x^{k+1}
     const float kcorr = pbf.scorr_k, ncorr = pbf.scorr_n;
     for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
         if (k == s) return true;
@@ -260,90 +361,114 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta(const float4* __restrict__
                 dscorr = -kcorr * ncorr * rn1 * (-3.0f * dp.kernel.poly6 * hr2 * hr2) / w_q;
         }
         const float lij = li + lam[k] + scorr;
-        const float lbar = dot3(Db, a);
+        const float3 Dbk = f3(Db[k]);
+        const float3 dDb = make_float3(Dbi.x - Dbk.x, Dbi.y - Dbk.y, Dbi.z - Dbk.z);
+        const float lbar = dot3(dDb, a);
         lown += lbar;
-        atomicAdd(lambar + k, lbar);
-        float3 ub = jt(q, make_float3(lij * Db.x, lij * Db.y, lij * Db.z));
+        float3 ub = jt(q, make_float3(lij * dDb.x, lij * dDb.y, lij * dDb.z));
         const float r2bar = lbar * dscorr;
-        ub.x += 2.f * q.u.x * r2bar;
-        ub.y += 2.f * q.u.y * r2bar;
-        ub.z += 2.f * q.u.z * r2bar;
-        own.x += ub.x;
-        own.y += ub.y;
-        own.z += ub.z;
-        atomic_add3(xbar_out + k, make_float3(-ub.x, -ub.y, -ub.z));
+        own.x += ub.x + 2.f * q.u.x * r2bar;
+        own.y += ub.y + 2.f * q.u.y * r2bar;
+        own.z += ub.z + 2.f * q.u.z * r2bar;
         return true;
     });
-    atomicAdd(lambar + s, lown);
-    atomic_add3(xbar_out + s, own);
+    lambar[s] = lown;
+    xbar_out[s] = make_float4(own.x, own.y, own.z, 0.f);
 }
 
 // ---------------------------------------------------------------- lambda
 // lambda_i = -(rho_i / rho0 - 1) / (scale^2 (sum_j |a_ij|^2 + |sum_j a_ij|^2) + eps)
-__global__ void __launch_bounds__(kAdjBS) k_adj_lambda(const float4* __restrict__ x,
-                                                       const float4* __restrict__ accs, Cand cand,
-                                                       const sim::DeviceParams* __restrict__ dpp, uint32_t N,
-                                                       const float* __restrict__ lambar,
-                                                       float4* __restrict__ xbar_out) {
+// First, per particle, from the recorded neighbour sums and dL/dlambda_i: the
+// coefficients of its pair terms, c0 = (G, sb), c1 = (rhob, bits of the slot
+// of its last counted neighbour), zero where the forward's branches pass no
+// gradient (lambda zeroed, not finite or clamped).
+__global__ void __launch_bounds__(kBS) k_adj_lambda_coef(const float4* __restrict__ accs,
+                                                         const float* __restrict__ lambar,
+                                                         const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                         float4* __restrict__ coef) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const sim::DeviceParams& dp = *dpp;
     const sim::PbfTuning& pbf = dp.pbf;
+    const float4 a0 = accs[2 * size_t(s)], a1 = accs[2 * size_t(s) + 1];
+    float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = make_float4(0.f, a1.z, 0.f, 0.f);
     const float lb_i = lambar[s];
-    if (lb_i == 0.f) return;
-    const float4 xi = x[s];
-    const int cap = dp.maxNeighbors > 0 ? dp.maxNeighbors : 0x7FFFFFFF;
-    // the forward's neighbour sums, as the replay recorded them
-    LambdaAcc acc;
-    {
-        const float4 a0 = accs[2 * size_t(s)], a1 = accs[2 * size_t(s) + 1];
-        acc.density = a0.x;
-        acc.sumGrad2 = a0.y;
-        acc.gx = a0.z;
-        acc.gy = a0.w;
-        acc.gz = a1.x;
-        acc.contrib = int(a1.y);
-    }
-    // the forward's branches (lambda_finalize)
     const float rho0 = dp.restDensity;
     const float scale = (rho0 > 0.f) ? dp.particleMass / rho0 : 0.f;
-    const float G2 = acc.gx * acc.gx + acc.gy * acc.gy + acc.gz * acc.gz;
-    const float sum = acc.sumGrad2 + G2;
+    const float gx = a0.z, gy = a0.w, gz = a1.x;
+    const float G2 = gx * gx + gy * gy + gz * gz;
+    const float sum = a0.y + G2;
     float denom0 = scale * scale * sum + pbf.lambda_denom_eps;
     if (pbf.compliance > 0.f && dp.dt > 0.f) denom0 += pbf.compliance / (dp.dt * dp.dt);
     const float denom = fmaxf(denom0, pbf.lambda_denom_eps);
-    if (acc.contrib < 2 || sum < 1e-12f || !(rho0 > 0.f)) return;
-    const float C = acc.density / rho0 - 1.f;
-    const float lam = -C / denom;
-    if (!isfinite(lam)) return;
-    if (pbf.enable_lambda_clamp && fabsf(lam) > pbf.lambda_max_abs) return;
-    const float Cb = -lb_i / denom;
-    const float denb = (denom0 >= pbf.lambda_denom_eps) ? -lb_i * lam / denom : 0.f;
-    const float sb = denb * scale * scale;
-    const float rhob = Cb / rho0;
-    const float3 G = make_float3(acc.gx, acc.gy, acc.gz);
-    float3 own = make_float3(0.f, 0.f, 0.f);
+    const int contrib = int(a1.y);
+    bool live = lb_i != 0.f && !(contrib < 2 || sum < 1e-12f || !(rho0 > 0.f));
+    float lam = 0.f;
+    if (live) {
+        lam = -(a0.x / rho0 - 1.f) / denom;
+        live = isfinite(lam) && !(pbf.enable_lambda_clamp && fabsf(lam) > pbf.lambda_max_abs);
+    }
+    if (live) {
+        const float Cb = -lb_i / denom;
+        const float denb = (denom0 >= pbf.lambda_denom_eps) ? -lb_i * lam / denom : 0.f;
+        c0 = make_float4(gx, gy, gz, denb * scale * scale);
+        c1.x = Cb / rho0;
+    }
+    coef[2 * size_t(s)] = c0;
+    coef[2 * size_t(s) + 1] = c1;
+}
+
+// Then each particle j gathers, over its neighbours k in walk order, the term
+// of its own equation (for its first maxNeighbors neighbours) and the term of
+// k's equation when j was among k's counted neighbours (walks visit slots in
+// ascending order, so: slot j <= k's last counted slot):
+//   dL/dx_j += J_jk^T (2 sb_j (a_jk + G_j)) + 2 u_jk rhob_j m W'(r2)
+//            - J_jk^T (2 sb_k (G_k - a_jk)) + 2 u_jk rhob_k m W'(r2).
+__global__ void __launch_bounds__(kAdjBS) k_adj_lambda_gather(const float4* __restrict__ x,
+                                                              const float4* __restrict__ coef, Cand cand,
+                                                              const sim::DeviceParams* __restrict__ dpp, uint32_t N,
+                                                              float4* __restrict__ xbar_out) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const sim::DeviceParams& dp = *dpp;
+    const float4 xi = x[s];
+    const int cap = dp.maxNeighbors > 0 ? dp.maxNeighbors : 0x7FFFFFFF;
+    const float4 ci0 = coef[2 * size_t(s)], ci1 = coef[2 * size_t(s) + 1];
+    const float3 Gi = f3(ci0);
+    const float sbi = ci0.w, rhobi = ci1.x;
+    const float mp6 = -3.0f * dp.particleMass * dp.kernel.poly6;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
     int seen = 0;
     for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
-        if (seen >= cap) return false;
         if (k == s) return true;
         const Pair q = pair_of(xi, x[k], dp);
         if (q.r2 > dp.kernel.h2) return true;
-        ++seen;
         const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
         const float hr2 = dp.kernel.h2 - q.r2;
-        const float r2bar = -3.0f * rhob * dp.particleMass * dp.kernel.poly6 * hr2 * hr2;
-        float3 ub = jt(q, make_float3(2.f * sb * (a.x + G.x), 2.f * sb * (a.y + G.y), 2.f * sb * (a.z + G.z)));
-        ub.x += 2.f * q.u.x * r2bar;
-        ub.y += 2.f * q.u.y * r2bar;
-        ub.z += 2.f * q.u.z * r2bar;
-        own.x += ub.x;
-        own.y += ub.y;
-        own.z += ub.z;
-        atomic_add3(xbar_out + k, make_float3(-ub.x, -ub.y, -ub.z));
+        const float dW = mp6 * hr2 * hr2;
+        if (seen < cap && (sbi != 0.f || rhobi != 0.f)) {
+            const float3 ub = jt(q, make_float3(2.f * sbi * (a.x + Gi.x), 2.f * sbi * (a.y + Gi.y),
+                                                2.f * sbi * (a.z + Gi.z)));
+            const float r2bar = rhobi * dW;
+            acc.x += ub.x + 2.f * q.u.x * r2bar;
+            acc.y += ub.y + 2.f * q.u.y * r2bar;
+            acc.z += ub.z + 2.f * q.u.z * r2bar;
+        }
+        ++seen;
+        const float4 ck0 = coef[2 * size_t(k)], ck1 = coef[2 * size_t(k) + 1];
+        if (s <= __float_as_uint(ck1.y) && (ck0.w != 0.f || ck1.x != 0.f)) {
+            const float sbk = ck0.w;
+            const float3 ub = jt(q, make_float3(2.f * sbk * (ck0.x - a.x), 2.f * sbk * (ck0.y - a.y),
+                                                2.f * sbk * (ck0.z - a.z)));
+            const float r2bar = ck1.x * dW;
+            acc.x += -ub.x + 2.f * q.u.x * r2bar;
+            acc.y += -ub.y + 2.f * q.u.y * r2bar;
+            acc.z += -ub.z + 2.f * q.u.z * r2bar;
+        }
         return true;
     });
-    atomic_add3(xbar_out + s, own);
+    const float4 o = xbar_out[s];
+    xbar_out[s] = make_float4(o.x + acc.x, o.y + acc.y, o.z + acc.z, 0.f);
 }
 
 // ---------------------------------------------------------------- predict
@@ -529,6 +654,9 @@ struct pbf_tape {
     float4 *pbar = nullptr, *vbar = nullptr, *xfbar = nullptr, *vxbar = nullptr, *vfbar = nullptr, *xbA = nullptr,
            *xbB = nullptr, *pbar_s = nullptr;
     float *lambar = nullptr, *cbar = nullptr;
+    float4* Db = nullptr;     // delta adjoint: clamp-projected gradient per particle
+    float4* lcoef = nullptr;  // lambda adjoint: pair-term coefficients, 2 per particle
+    float* cpart = nullptr;   // XSPH adjoint: per-block partials of dL/dc
     uint32_t* listStats = nullptr;
     uint32_t listCap = 0;  // 0: the replay walks the stencil
     int listSpan = 0;
@@ -617,9 +745,12 @@ struct pbf_tape {
         k_adj_gather_out<<<g, kBS, 0, stream>>>(r.perm, pbar, vbar, N, xfbar, vxbar);
         const float4* xf = r.x[std::max(iters, 0)];
         const Cand cand{r.key_s, r.lb, r.list, r.count, listCap};
-        if (xsph) {
+        if (xsph && p.pbf.xsph_gate_enable) {
             cudaMemsetAsync(vfbar, 0, b4, stream);
             k_adj_xsph<<<ga, kAdjBS, 0, stream>>>(xf, r.vf, cand, dp, N, vxbar, vfbar, xfbar, cbar);
+        } else if (xsph) {
+            k_adj_xsph_gather<<<ga, kAdjBS, 0, stream>>>(xf, r.vf, cand, dp, N, vxbar, vfbar, xfbar, cpart);
+            k_sum_partials<<<1, 256, 0, stream>>>(cpart, ga, cbar);
         } else {
             cudaMemcpyAsync(vfbar, vxbar, b4, cudaMemcpyDeviceToDevice, stream);
         }
@@ -627,10 +758,10 @@ struct pbf_tape {
         float4* xin = xbA;
         float4* xout = xbB;
         for (int it = iters - 1; it >= 0; --it) {
-            cudaMemsetAsync(xout, 0, b4, stream);
-            cudaMemsetAsync(lambar, 0, sizeof(float) * N, stream);
-            k_adj_delta<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], r.D[it], cand, dp, N, xin, xout, lambar);
-            k_adj_lambda<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.A[it], cand, dp, N, lambar, xout);
+            k_adj_delta_db<<<g, kBS, 0, stream>>>(r.D[it], xin, dp, N, Db);
+            k_adj_delta_gather<<<ga, kAdjBS, 0, stream>>>(r.x[it], r.lam[it], Db, cand, dp, N, xin, xout, lambar);
+            k_adj_lambda_coef<<<g, kBS, 0, stream>>>(r.A[it], lambar, dp, N, lcoef);
+            k_adj_lambda_gather<<<ga, kAdjBS, 0, stream>>>(r.x[it], lcoef, cand, dp, N, xout);
             std::swap(xin, xout);
         }
         k_adj_predict<<<g, kBS, 0, stream>>>(r.x[0], xin, pbar_s, r.perm, dp, N, pbar, vbar);
@@ -674,6 +805,8 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
               t->alloc(reinterpret_cast<unsigned char**>(&t->sortTemp), t->sortBytes) && t->alloc(&t->pbar, N) &&
               t->alloc(&t->vbar, N) && t->alloc(&t->xfbar, N) && t->alloc(&t->vxbar, N) && t->alloc(&t->vfbar, N) &&
               t->alloc(&t->xbA, N) && t->alloc(&t->xbB, N) && t->alloc(&t->pbar_s, N) && t->alloc(&t->lambar, N) &&
+              t->alloc(&t->Db, N) && t->alloc(&t->lcoef, 2 * size_t(N)) &&
+              t->alloc(&t->cpart, size_t(blocks_for(N, kAdjBS))) &&
               t->alloc(&t->cbar, 1) && t->alloc(&t->listStats, 2);
     for (int c = 0; ok && c < segs; ++c) {
         float4 *cp = nullptr, *cv = nullptr;

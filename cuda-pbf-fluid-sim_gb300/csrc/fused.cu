@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     // the neighbour sums, for the adjoint's replay
     if (acc_out) {
         acc_out[2 * size_t(s)] = make_float4(a.density, a.sumGrad2, a.gx, a.gy);
-        acc_out[2 * size_t(s) + 1] = make_float4(a.gz, float(a.contrib), 0.f, 0.f);
+        acc_out[2 * size_t(s) + 1] = make_float4(a.gz, float(a.contrib), __uint_as_float(a.last), 0.f);
     }
     lam[s] = lambda_finalize(a, dp);
 }

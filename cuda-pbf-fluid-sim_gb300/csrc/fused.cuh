@@ -33,7 +33,8 @@ struct FusedBufs {
     // slot, before the displacement clamp (the adjoint's replay records it).
     float4* delta_sum;
     // Optional: the lambda pass's neighbour sums per sorted slot, two float4
-    // each: (density, sum |grad|^2, grad x, grad y), (grad z, contributions).
+    // each: (density, sum |grad|^2, grad x, grad y), (grad z, contributions,
+    // bits of the last neighbour's index, 0).
     float4* lambda_acc;
     float4* pos_s;
     float4* vel_s;

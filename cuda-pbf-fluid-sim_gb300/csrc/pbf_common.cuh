@@ -531,6 +531,7 @@ struct CompactRows {
 struct LambdaAcc {
     float density = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, sumGrad2 = 0.f;
     int contrib = 0;
+    uint32_t last = 0;  // candidate index of the last neighbour summed (walks visit them in slot order)
 };
 
 __device__ __forceinline__ void lambda_accumulate(LambdaAcc& a, float rx, float ry, float rz, float r2,
@@ -587,6 +588,7 @@ __device__ __forceinline__ LambdaAcc lambda_of_acc(uint32_t self, float4 pi, int
         const float r2 = dist2(pi, pj, rx, ry, rz);
         if (r2 > dp.kernel.h2) return true;
         lambda_accumulate(a, rx, ry, rz, r2, dp);
+        a.last = j;
         return true;
     });
     return a;
@@ -619,6 +621,7 @@ __device__ __forceinline__ LambdaAcc lambda_queued_acc(bool active, uint32_t s, 
             float rx, ry, rz;
             const float r2 = dist2(pi, data.p(k), rx, ry, rz);
             lambda_accumulate(a, rx, ry, rz, r2, dp);
+            a.last = k;
         });
     return a;
 }

@@ -167,6 +167,40 @@ def test_checkpoint_interval_does_not_change_gradients(gpu, lib, problem):
         assert got[3] == pytest.approx(ref[3], rel=1e-4)
 
 
+@pytest.mark.gpu
+def test_backward_is_deterministic(gpu, lib, problem):
+    """Every particle gathers its terms (no atomics, XSPH gate off): two
+    backward passes over the same tape and loss gradient give the same bits."""
+    torch = gpu
+    p, pos, vel, target, steps, _ = problem
+    n = pos.shape[0]
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        s.upload(pos, vel)
+        tape = C.c_void_p()
+        pbfx.check(lib.pbf_forward(s.h, steps, 1, C.byref(tape)), "forward")
+        try:
+            tgt = torch.tensor(target, dtype=torch.float32, device="cuda")
+            pbar = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+            vbar = torch.zeros_like(pbar)
+            loss = C.c_double()
+            pbfx.check(lib.pbf_density_grid_loss(s.h, RES, C.c_void_p(tgt.data_ptr()), C.byref(loss),
+                                                 C.c_void_p(pbar.data_ptr())), "loss")
+            out = []
+            for _ in range(2):
+                p0, v0 = torch.zeros_like(pbar), torch.zeros_like(pbar)
+                cb = C.c_float()
+                pbfx.check(lib.pbf_backward(tape, C.c_void_p(pbar.data_ptr()), C.c_void_p(vbar.data_ptr()),
+                                            C.c_void_p(p0.data_ptr()), C.c_void_p(v0.data_ptr()), C.byref(cb)),
+                           "backward")
+                out.append((p0.cpu().numpy(), v0.cpu().numpy(), cb.value))
+        finally:
+            lib.pbf_tape_destroy(tape)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    assert np.abs(out[0][1]).max() > 0
+
+
 def test_adjoint_rejects_bad_arguments(lib):
     t = C.c_void_p()
     assert lib.pbf_forward(None, 4, 2, C.byref(t)) == pbfx.PBF_ERR_INVALID
