@@ -109,6 +109,33 @@ __device__ __forceinline__ void for_candidates(uint32_t s, const Cand& c, const 
     walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{c.lb}, visit);
 }
 
+// The same candidates with the forward passes' queued warp walk: each lane
+// queues its hits (hit(k), the cheap test) in a shared-memory ring and the
+// warp runs the bodies in bulk, each lane in its own walk order.  A warp walks
+// the stencil rows when any of its lists overflowed or none was kept.  Every
+// lane of the warp calls it; q is the lane's queue (kAdjQ entries, stride
+// kAdjBS).
+constexpr int kAdjQ = 32;
+template <class Hit, class Body>
+__device__ __forceinline__ void adj_walk(bool active, uint32_t s, const Cand& c, const sim::DeviceParams& dp,
+                                         uint32_t* q, Hit&& hit, Body&& body) {
+    uint32_t n = 0;
+    bool lists = c.list != nullptr;
+    if (lists) {
+        n = active ? c.count[s] : 0u;
+        lists = !__any_sync(0xFFFFFFFFu, n > c.cap);
+    }
+    if (lists) {
+        walk_list_queued<kAdjQ, kAdjBS>(active, ListSource<uint32_t>{c.list + size_t(s) * c.cap, n, s}, q,
+                                        0x7FFFFFFF, hit, body);
+    } else {
+        int cx, cy, cz;
+        decode_key(c.key_s[s], dp.grid.dim, cx, cy, cz);
+        walk_queued<kAdjQ, kAdjBS>(active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{c.lb}, q,
+                                   0x7FFFFFFF, hit, body);
+    }
+}
+
 // ---------------------------------------------------------------- XSPH
 // v''_i = v_i + c g (m / rho0) sum_j (v_j - v_i) W_ij at the solved positions.
 __global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ xf, const float4* __restrict__ vf,
@@ -182,27 +209,32 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_xsph(const float4* __restrict__ 
 //   dL/dx_j += sum_k 2 (x_j - x_k) c W'(r2) (v_k - v_j) . (g_j - g_k),
 // with W'(r2) = -3 poly6 (h^2 - r2)^2, and its part of dL/dc in a per-block
 // partial (summed in a fixed order by k_sum_partials).
-__global__ void __launch_bounds__(kAdjBS) k_adj_xsph_gather(const float4* __restrict__ xf,
+__global__ void __launch_bounds__(kAdjBS, 6) k_adj_xsph_gather(const float4* __restrict__ xf,
                                                             const float4* __restrict__ vf, Cand cand,
                                                             const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                             const float4* __restrict__ vbar_out,
                                                             float4* __restrict__ vfbar, float4* __restrict__ xfbar,
                                                             float* __restrict__ cpart_blocks) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    float cpart = 0.f;
-    if (s < N) {
-        const sim::DeviceParams& dp = *dpp;
-        const float4 xi = xf[s], vi = vf[s];
-        const float3 g = f3(vbar_out[s]);
-        const float mor = (dp.restDensity > 0.f) ? dp.particleMass / dp.restDensity : 0.f;
-        const float ceff = dp.xsph_c * mor;
-        float wsum = 0.f;
-        float3 sum = make_float3(0.f, 0.f, 0.f), gsum = make_float3(0.f, 0.f, 0.f), xb = make_float3(0.f, 0.f, 0.f);
-        for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
-            if (k == s) return true;
+    __shared__ uint32_t qs[kAdjQ * kAdjBS];
+    const uint32_t s0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = s0 < N;  // every lane takes part in the warp-wide walk
+    const uint32_t s = active ? s0 : 0u;
+    const sim::DeviceParams dp = *dpp;
+    const float4 xi = xf[s], vi = vf[s];
+    const float3 g = f3(vbar_out[s]);
+    const float mor = (dp.restDensity > 0.f) ? dp.particleMass / dp.restDensity : 0.f;
+    const float ceff = dp.xsph_c * mor;
+    float wsum = 0.f;
+    float3 sum = make_float3(0.f, 0.f, 0.f), gsum = make_float3(0.f, 0.f, 0.f), xb = make_float3(0.f, 0.f, 0.f);
+    adj_walk(
+        active, s, cand, dp, qs + threadIdx.x,
+        [&](uint32_t k) -> bool {
+            float rx, ry, rz;
+            return k != s && !(dist2(xi, xf[k], rx, ry, rz) > dp.kernel.h2);
+        },
+        [&](uint32_t k) {
             float rx, ry, rz;
             const float r2 = dist2(xi, xf[k], rx, ry, rz);
-            if (r2 > dp.kernel.h2) return true;
             const float hr2 = sub_(dp.kernel.h2, r2);
             const float w = mul_(mul_(mul_(dp.kernel.poly6, hr2), hr2), hr2);
             const float4 vj = vf[k];
@@ -220,8 +252,9 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_xsph_gather(const float4* __rest
             xb.x += 2.f * rx * r2bar;
             xb.y += 2.f * ry * r2bar;
             xb.z += 2.f * rz * r2bar;
-            return true;
         });
+    float cpart = 0.f;
+    if (active) {
         cpart = mor * dot3(sum, g);
         vfbar[s] = make_float4(g.x - ceff * wsum * g.x + ceff * gsum.x, g.y - ceff * wsum * g.y + ceff * gsum.y,
                                g.z - ceff * wsum * g.z + ceff * gsum.z, 0.f);
@@ -315,16 +348,18 @@ __global__ void __launch_bounds__(kBS) k_adj_delta_db(const float4* __restrict__
 //   dL/dx^k_j = dL/dx^{k+1}_j + sum_k [J_jk^T (l_jk dDb) + 2 u_jk (dDb . a_jk) dscorr/dr2],
 // both equations' terms of the pair at once (a_kj = -a_jk, the same l, s_corr
 // and Jacobian).
-__global__ void __launch_bounds__(kAdjBS) k_adj_delta_gather(const float4* __restrict__ x,
+__global__ void __launch_bounds__(kAdjBS, 6) k_adj_delta_gather(const float4* __restrict__ x,
                                                              const float* __restrict__ lam,
                                                              const float4* __restrict__ Db, Cand cand,
                                                              const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                              const float4* __restrict__ xbar_in,
                                                              float4* __restrict__ xbar_out,
                                                              float* __restrict__ lambar) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= N) return;
-    const sim::DeviceParams& dp = *dpp;
+    __shared__ uint32_t qs[kAdjQ * kAdjBS];
+    const uint32_t s0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = s0 < N;  // every lane takes part in the warp-wide walk
+    const uint32_t s = active ? s0 : 0u;
+    const sim::DeviceParams dp = *dpp;
     const sim::PbfTuning& pbf = dp.pbf;
     const float4 xi = x[s];
     const float li = lam[s];
@@ -333,45 +368,49 @@ __global__ void __launch_bounds__(kAdjBS) k_adj_delta_gather(const float4* __res
     float lown = 0.f;
     float3 own = f3(xbar_in[s]);  // identity path x^k -> x^{k+1}
     const float kcorr = pbf.scorr_k, ncorr = pbf.scorr_n;
-    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
-        if (k == s) return true;
-        const Pair q = pair_of(xi, x[k], dp);
-        if (q.r2 > dp.kernel.h2) return true;
-        const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
-        float scorr = 0.f, dscorr = 0.f;  // d scorr / d r2
-        if (pbf.scorr_enable) {
-            const float hr2 = dp.kernel.h2 - q.r2;
-            const float w = dp.kernel.poly6 * hr2 * hr2 * hr2;
-            const float ratio = (w_q > 0.f) ? w / w_q : 0.f;
-            // ratio^n and ratio^(n-1); products for the default n = 4 (the
-            // adjoint is FP32 calculus, not a replay of the forward's bits)
-            float rn, rn1;
-            if (ncorr == 4.0f) {
-                const float q2 = ratio * ratio;
-                rn1 = q2 * ratio;
-                rn = q2 * q2;
-            } else {
-                rn = powf(ratio, ncorr);
-                rn1 = powf(ratio, ncorr - 1.0f);
+    adj_walk(
+        active, s, cand, dp, qs + threadIdx.x,
+        [&](uint32_t k) -> bool {
+            float rx, ry, rz;
+            return k != s && !(dist2(xi, x[k], rx, ry, rz) > dp.kernel.h2);
+        },
+        [&](uint32_t k) {
+            const Pair q = pair_of(xi, x[k], dp);
+            const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
+            float scorr = 0.f, dscorr = 0.f;  // d scorr / d r2
+            if (pbf.scorr_enable) {
+                const float hr2 = dp.kernel.h2 - q.r2;
+                const float w = dp.kernel.poly6 * hr2 * hr2 * hr2;
+                const float ratio = (w_q > 0.f) ? w / w_q : 0.f;
+                // ratio^n and ratio^(n-1); products for the default n = 4 (the
+                // adjoint is FP32 calculus, not a replay of the forward's bits)
+                float rn, rn1;
+                if (ncorr == 4.0f) {
+                    const float q2 = ratio * ratio;
+                    rn1 = q2 * ratio;
+                    rn = q2 * q2;
+                } else {
+                    rn = powf(ratio, ncorr);
+                    rn1 = powf(ratio, ncorr - 1.0f);
+                }
+                scorr = -kcorr * rn;
+                const bool floored = pbf.scorr_min < 0.f && scorr < pbf.scorr_min;
+                if (floored) scorr = pbf.scorr_min;
+                if (!floored && w_q > 0.f && ratio > 0.f)
+                    dscorr = -kcorr * ncorr * rn1 * (-3.0f * dp.kernel.poly6 * hr2 * hr2) / w_q;
             }
-            scorr = -kcorr * rn;
-            const bool floored = pbf.scorr_min < 0.f && scorr < pbf.scorr_min;
-            if (floored) scorr = pbf.scorr_min;
-            if (!floored && w_q > 0.f && ratio > 0.f)
-                dscorr = -kcorr * ncorr * rn1 * (-3.0f * dp.kernel.poly6 * hr2 * hr2) / w_q;
-        }
-        const float lij = li + lam[k] + scorr;
-        const float3 Dbk = f3(Db[k]);
-        const float3 dDb = make_float3(Dbi.x - Dbk.x, Dbi.y - Dbk.y, Dbi.z - Dbk.z);
-        const float lbar = dot3(dDb, a);
-        lown += lbar;
-        float3 ub = jt(q, make_float3(lij * dDb.x, lij * dDb.y, lij * dDb.z));
-        const float r2bar = lbar * dscorr;
-        own.x += ub.x + 2.f * q.u.x * r2bar;
-        own.y += ub.y + 2.f * q.u.y * r2bar;
-        own.z += ub.z + 2.f * q.u.z * r2bar;
-        return true;
-    });
+            const float lij = li + lam[k] + scorr;
+            const float3 Dbk = f3(Db[k]);
+            const float3 dDb = make_float3(Dbi.x - Dbk.x, Dbi.y - Dbk.y, Dbi.z - Dbk.z);
+            const float lbar = dot3(dDb, a);
+            lown += lbar;
+            const float3 ub = jt(q, make_float3(lij * dDb.x, lij * dDb.y, lij * dDb.z));
+            const float r2bar = lbar * dscorr;
+            own.x += ub.x + 2.f * q.u.x * r2bar;
+            own.y += ub.y + 2.f * q.u.y * r2bar;
+            own.z += ub.z + 2.f * q.u.z * r2bar;
+        });
+    if (!active) return;
     lambar[s] = lown;
     xbar_out[s] = make_float4(own.x, own.y, own.z, 0.f);
 }
@@ -424,49 +463,56 @@ __global__ void __launch_bounds__(kBS) k_adj_lambda_coef(const float4* __restric
 // ascending order, so: slot j <= k's last counted slot):
 //   dL/dx_j += J_jk^T (2 sb_j (a_jk + G_j)) + 2 u_jk rhob_j m W'(r2)
 //            - J_jk^T (2 sb_k (G_k - a_jk)) + 2 u_jk rhob_k m W'(r2).
-__global__ void __launch_bounds__(kAdjBS) k_adj_lambda_gather(const float4* __restrict__ x,
+__global__ void __launch_bounds__(kAdjBS, 6) k_adj_lambda_gather(const float4* __restrict__ x,
                                                               const float4* __restrict__ coef, Cand cand,
                                                               const sim::DeviceParams* __restrict__ dpp, uint32_t N,
                                                               float4* __restrict__ xbar_out) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= N) return;
-    const sim::DeviceParams& dp = *dpp;
+    __shared__ uint32_t qs[kAdjQ * kAdjBS];
+    const uint32_t s0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = s0 < N;  // every lane takes part in the warp-wide walk
+    const uint32_t s = active ? s0 : 0u;
+    const sim::DeviceParams dp = *dpp;
     const float4 xi = x[s];
     const int cap = dp.maxNeighbors > 0 ? dp.maxNeighbors : 0x7FFFFFFF;
     const float4 ci0 = coef[2 * size_t(s)], ci1 = coef[2 * size_t(s) + 1];
     const float3 Gi = f3(ci0);
     const float sbi = ci0.w, rhobi = ci1.x;
+    const bool liveI = sbi != 0.f || rhobi != 0.f;
     const float mp6 = -3.0f * dp.particleMass * dp.kernel.poly6;
     float3 acc = make_float3(0.f, 0.f, 0.f);
     int seen = 0;
-    for_candidates(s, cand, dp, [&](uint32_t k) -> bool {
-        if (k == s) return true;
-        const Pair q = pair_of(xi, x[k], dp);
-        if (q.r2 > dp.kernel.h2) return true;
-        const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
-        const float hr2 = dp.kernel.h2 - q.r2;
-        const float dW = mp6 * hr2 * hr2;
-        if (seen < cap && (sbi != 0.f || rhobi != 0.f)) {
-            const float3 ub = jt(q, make_float3(2.f * sbi * (a.x + Gi.x), 2.f * sbi * (a.y + Gi.y),
-                                                2.f * sbi * (a.z + Gi.z)));
-            const float r2bar = rhobi * dW;
-            acc.x += ub.x + 2.f * q.u.x * r2bar;
-            acc.y += ub.y + 2.f * q.u.y * r2bar;
-            acc.z += ub.z + 2.f * q.u.z * r2bar;
-        }
-        ++seen;
-        const float4 ck0 = coef[2 * size_t(k)], ck1 = coef[2 * size_t(k) + 1];
-        if (s <= __float_as_uint(ck1.y) && (ck0.w != 0.f || ck1.x != 0.f)) {
-            const float sbk = ck0.w;
-            const float3 ub = jt(q, make_float3(2.f * sbk * (ck0.x - a.x), 2.f * sbk * (ck0.y - a.y),
-                                                2.f * sbk * (ck0.z - a.z)));
-            const float r2bar = ck1.x * dW;
-            acc.x += -ub.x + 2.f * q.u.x * r2bar;
-            acc.y += -ub.y + 2.f * q.u.y * r2bar;
-            acc.z += -ub.z + 2.f * q.u.z * r2bar;
-        }
-        return true;
-    });
+    adj_walk(
+        active, s, cand, dp, qs + threadIdx.x,
+        [&](uint32_t k) -> bool {
+            float rx, ry, rz;
+            return k != s && !(dist2(xi, x[k], rx, ry, rz) > dp.kernel.h2);
+        },
+        [&](uint32_t k) {
+            const Pair q = pair_of(xi, x[k], dp);
+            const float3 a = make_float3(q.coeff * q.u.x, q.coeff * q.u.y, q.coeff * q.u.z);
+            const float hr2 = dp.kernel.h2 - q.r2;
+            const float dW = mp6 * hr2 * hr2;
+            if (seen < cap && liveI) {
+                const float3 ub = jt(q, make_float3(2.f * sbi * (a.x + Gi.x), 2.f * sbi * (a.y + Gi.y),
+                                                    2.f * sbi * (a.z + Gi.z)));
+                const float r2bar = rhobi * dW;
+                acc.x += ub.x + 2.f * q.u.x * r2bar;
+                acc.y += ub.y + 2.f * q.u.y * r2bar;
+                acc.z += ub.z + 2.f * q.u.z * r2bar;
+            }
+            ++seen;
+            const float4 ck0 = coef[2 * size_t(k)], ck1 = coef[2 * size_t(k) + 1];
+            if (s <= __float_as_uint(ck1.y) && (ck0.w != 0.f || ck1.x != 0.f)) {
+                const float sbk = ck0.w;
+                const float3 ub = jt(q, make_float3(2.f * sbk * (ck0.x - a.x), 2.f * sbk * (ck0.y - a.y),
+                                                    2.f * sbk * (ck0.z - a.z)));
+                const float r2bar = ck1.x * dW;
+                acc.x += -ub.x + 2.f * q.u.x * r2bar;
+                acc.y += -ub.y + 2.f * q.u.y * r2bar;
+                acc.z += -ub.z + 2.f * q.u.z * r2bar;
+            }
+        });
+    if (!active) return;
     const float4 o = xbar_out[s];
     xbar_out[s] = make_float4(o.x + acc.x, o.y + acc.y, o.z + acc.z, 0.f);
 }
