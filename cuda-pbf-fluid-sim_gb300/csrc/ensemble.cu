@@ -373,8 +373,7 @@ int pbf_ensemble_autotune(pbf_ensemble* e, int steps, float* ms, int* chosen) {
         return cudaMemcpyAsync(e->pos, snap, bytes, cudaMemcpyDeviceToDevice, e->stream) == cudaSuccess &&
                cudaMemcpyAsync(e->vel, snap + e->N, bytes, cudaMemcpyDeviceToDevice, e->stream) == cudaSuccess;
     };
-    int best = before;
-    float bestMs = 0.f;
+    std::vector<float> times(size_t(shapes), 0.f);
     for (int id = 0; st == PBF_OK && id < shapes; ++id) {
         if ((st = e->set_tile(id)) != PBF_OK) break;
         bool ok = cudaGraphLaunch(e->exec, e->stream) == cudaSuccess && restore() &&
@@ -387,13 +386,10 @@ int pbf_ensemble_autotune(pbf_ensemble* e, int steps, float* ms, int* chosen) {
             st = PBF_ERR_CUDA;
             break;
         }
-        t /= float(steps);
-        if (ms) ms[id] = t;
-        if (id == 0 || t < bestMs) {
-            best = id;
-            bestMs = t;
-        }
+        times[size_t(id)] = t / float(steps);
+        if (ms) ms[id] = times[size_t(id)];
     }
+    const int best = (st == PBF_OK) ? pbf::pick_tile_shape(times.data(), shapes, before) : before;
     if (snap && !(restore() && cudaStreamSynchronize(e->stream) == cudaSuccess) && st == PBF_OK) st = PBF_ERR_CUDA;
     const int st2 = e->set_tile(st == PBF_OK ? best : before);
     if (st == PBF_OK) st = st2;

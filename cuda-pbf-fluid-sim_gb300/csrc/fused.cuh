@@ -85,6 +85,18 @@ struct FusedShape {
 constexpr int kTileShapeCount = 4;
 int fused_tile_shape_count();
 bool fused_tile_shape_info(int id, int& tile, int& stage);
+// The autotuner's choice among measured step times: the fastest shape, but
+// the current one is kept unless the fastest beats it by kTileShapeMargin (a
+// few steps of one state do not rank shapes that close).
+constexpr float kTileShapeMargin = 0.02f;
+inline int pick_tile_shape(const float* ms, int n, int current) {
+    int best = (current >= 0 && current < n) ? current : 0;
+    for (int i = 0; i < n; ++i)
+        if (ms[i] < ms[best]) best = i;
+    if (best != current && current >= 0 && current < n && !(ms[best] < ms[current] * (1.0f - kTileShapeMargin)))
+        return current;
+    return best;
+}
 
 // Iterations a list may cover for these parameters: the list radius grows by
 // 2 * disp_clamp_max_h * h per covered position update; lists are rebuilt

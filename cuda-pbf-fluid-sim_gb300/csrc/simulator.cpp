@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <random>
+#include <vector>
 
 #include "fused.cuh"
 #include "grid.cuh"
@@ -439,8 +440,7 @@ bool Simulator::autotuneTileShape(const SimParams& p, int steps, float* ms) {
         return cudaMemcpyAsync(m_bufs.d_pos, snap, bytes, cudaMemcpyDeviceToDevice, m_stream) == cudaSuccess &&
                cudaMemcpyAsync(m_bufs.d_vel, snap + n, bytes, cudaMemcpyDeviceToDevice, m_stream) == cudaSuccess;
     };
-    int best = before;
-    float bestMs = 0.f;
+    std::vector<float> times(size_t(shapes), 0.f);
     for (int id = 0; ok && id < shapes; ++id) {
         // one untimed step captures the shape's graph
         ok = setTileShape(id) && step(p) && restore() && cudaEventRecord(e0, m_stream) == cudaSuccess;
@@ -449,16 +449,13 @@ bool Simulator::autotuneTileShape(const SimParams& p, int steps, float* ms) {
         ok = ok && cudaEventRecord(e1, m_stream) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
              cudaEventElapsedTime(&t, e0, e1) == cudaSuccess && restore();
         if (!ok) break;
-        t /= float(steps);
-        if (ms) ms[id] = t;
-        if (id == 0 || t < bestMs) {
-            best = id;
-            bestMs = t;
-        }
+        times[size_t(id)] = t / float(steps);
+        if (ms) ms[id] = times[size_t(id)];
     }
+    const int best = ok ? pbf::pick_tile_shape(times.data(), shapes, before) : before;
     if (snap) ok = restore() && cudaStreamSynchronize(m_stream) == cudaSuccess && ok;
     m_frameIndex = frame;
-    setTileShape(ok ? best : before);
+    setTileShape(best);
     uint32_t l = 0, o = 0;
     neighbourListStats(l, o, true);
     if (e0) cudaEventDestroy(e0);

@@ -35,6 +35,14 @@ def run(lib, p, pos, vel, hashed, shape, steps, cap=None):
         return gp, gv, s.fetch(pbfx.DBG_LAMBDA)
 
 
+def kept_or_fastest(ms, chosen, before):
+    """The tuner keeps the current shape unless another is at least 2% faster."""
+    best = min(range(len(ms)), key=lambda i: ms[i])
+    if ms[best] < ms[before] * 0.98:
+        return chosen == best
+    return chosen == before
+
+
 def assert_same(a, b):
     for x, y, what in zip(a, b, ("positions", "velocities", "lambda")):
         np.testing.assert_array_equal(x, y, err_msg=what)
@@ -84,7 +92,7 @@ def test_autotune_restores_the_state(gpu, lib):
         assert_same(after, before[:2])
         assert s.tile_shape() == chosen
         assert len(ms) == len(pbfx.tile_shapes(lib)) and all(m > 0 for m in ms)
-        assert ms[chosen] == min(ms)
+        assert kept_or_fastest(ms, chosen, 0)
         s.step(5)
         tuned = s.download()
     untuned = run(lib, p, pos, vel, True, 0, 10)
@@ -110,7 +118,7 @@ def test_ensemble_shapes_and_autotune(gpu, lib):
         before = e.download()
         chosen, ms = e.autotune(steps=2)
         assert_same(e.download(), before)
-        assert e.tile_shape() == chosen and ms[chosen] == min(ms)
+        assert e.tile_shape() == chosen and kept_or_fastest(ms, chosen, 0)
         e.step(10)
         assert_same(e.download(), out[0])
         with pytest.raises(RuntimeError):
