@@ -26,10 +26,8 @@ namespace pbf {
 namespace {
 
 constexpr int kBS = 256;
-// Neighbour kernels: 128 threads, a 32-entry neighbour queue per thread in
-// shared memory (16 KB per block), column-major so a warp's queue writes hit
-// 32 distinct banks.
-constexpr int kNbrBS = 128;
+// Neighbour walks: a 32-entry ring queue per thread in shared memory,
+// column-major so a warp's queue writes hit 32 distinct banks.
 constexpr int kQueue = 32;
 
 __global__ void __launch_bounds__(kBS) k_predict_keys(const float4* __restrict__ pos, const float4* __restrict__ vel,

@@ -45,26 +45,57 @@ __global__ void k_cell_lb_mark(uint32_t* __restrict__ lb, const uint32_t* __rest
     }
 }
 
-// Pass two, a thread per cell in warps of 32 consecutive cells: an empty cell
-// takes the value of the next cell with particles (no key lies between
-// them); in the warp's window that is a shuffle from the next marked lane,
-// past it one binary search for the first cell after the window.  Lanes past
-// the table count as marked with N, which only matters when N = 0.
+// Pass two, a warp per block of 32 windows of 32 consecutive cells: an empty
+// cell takes the value of the next cell with particles (no key lies between
+// them).  The warp first finds each window's first marked value (lane j holds
+// window j's), then each window's carry, the first marked value of a later
+// window in the block, with a reverse shuffle scan; only a block whose tail
+// has no marked cell searches the keys, once, for the first cell after it.
+// Inside a window an empty cell takes the next marked lane's value by shuffle.
+// Cells past the table count as marked with N, which only matters when N = 0.
+constexpr uint32_t kLbBlockCells = 1024;
 __global__ void k_cell_lb_fill(uint32_t* __restrict__ lb, const uint32_t* __restrict__ keys, uint32_t N,
                                uint32_t numCells) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t v = c <= numCells ? lb[c] : N;
-    const uint32_t marked = __ballot_sync(0xFFFFFFFFu, v != kLbUnset);
-    const uint32_t after = marked & (0xFFFFFFFFu << lane);  // marked lanes at or after this one
-    uint32_t carry = 0;
-    if (__any_sync(0xFFFFFFFFu, after == 0u)) {
-        const uint32_t cEnd = c - lane + 32u;  // first cell after the window (<= numCells here)
-        if (lane == 0) carry = lower_bound_keys(keys, N, cEnd);
-        carry = __shfl_sync(0xFFFFFFFFu, carry, 0);
+    const uint64_t warp = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t base = warp * kLbBlockCells;
+    if (base > numCells) return;  // warp-uniform
+    // window firsts: lane j <- first marked value of window j (kLbUnset if none)
+    uint32_t first = kLbUnset;
+#pragma unroll 4
+    for (uint32_t j = 0; j < 32u; ++j) {
+        const uint64_t c = base + 32u * j + lane;
+        const uint32_t v = c <= numCells ? lb[c] : N;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, v != kLbUnset);
+        const uint32_t f = __shfl_sync(0xFFFFFFFFu, v, m ? int(__ffs(m)) - 1 : 0);
+        if (lane == j) first = m ? f : kLbUnset;
     }
-    const uint32_t next = __shfl_sync(0xFFFFFFFFu, v, int(__ffs(after)) - 1);
-    if (c <= numCells && v == kLbUnset) lb[c] = after ? next : carry;
+    // carry of window j: the first marked value of windows j + 1 .. 31, or past the block
+    uint32_t later = __shfl_down_sync(0xFFFFFFFFu, first, 1);
+    if (lane == 31u) later = kLbUnset;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_down_sync(0xFFFFFFFFu, later, o);
+        if (later == kLbUnset && lane + uint32_t(o) < 32u) later = t;
+    }
+    if (__any_sync(0xFFFFFFFFu, later == kLbUnset)) {
+        // first cell after the block (<= numCells wherever a lane needs it)
+        uint32_t past = 0;
+        if (lane == 0) past = base + kLbBlockCells <= numCells ? lower_bound_keys(keys, N, uint32_t(base + kLbBlockCells)) : N;
+        past = __shfl_sync(0xFFFFFFFFu, past, 0);
+        if (later == kLbUnset) later = past;
+    }
+    // fill
+#pragma unroll 4
+    for (uint32_t j = 0; j < 32u; ++j) {
+        const uint64_t c = base + 32u * j + lane;
+        const uint32_t v = c <= numCells ? lb[c] : N;
+        const uint32_t marked = __ballot_sync(0xFFFFFFFFu, v != kLbUnset);
+        const uint32_t after = marked & (0xFFFFFFFFu << lane);  // marked lanes at or after this one
+        const uint32_t next = __shfl_sync(0xFFFFFFFFu, v, after ? int(__ffs(after)) - 1 : 0);
+        const uint32_t carry = __shfl_sync(0xFFFFFFFFu, later, int(j));
+        if (c <= numCells && v == kLbUnset) lb[c] = after ? next : carry;
+    }
 }
 
 __global__ void k_cell_ranges_ref(uint32_t* __restrict__ start, uint32_t* __restrict__ end,
@@ -268,7 +299,8 @@ cudaError_t launch_cell_lb(uint32_t* lb, const uint32_t* keys_sorted, uint32_t N
     cudaError_t e = cudaMemsetAsync(lb, 0xFF, (size_t(numCells) + 1u) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     if (N > 0) k_cell_lb_mark<<<blocks_for(N, 256), 256, 0, s>>>(lb, keys_sorted, N, numCells);
-    k_cell_lb_fill<<<blocks_for(uint64_t(numCells) + 1u, 256), 256, 0, s>>>(lb, keys_sorted, N, numCells);
+    const uint64_t warps = (uint64_t(numCells) + kLbBlockCells) / kLbBlockCells;  // numCells + 1 cells
+    k_cell_lb_fill<<<blocks_for(warps * 32u, 256), 256, 0, s>>>(lb, keys_sorted, N, numCells);
     return cudaGetLastError();
 }
 
