@@ -126,12 +126,12 @@ __device__ __forceinline__ void adj_walk(bool active, uint32_t s, const Cand& c,
         lists = !__any_sync(0xFFFFFFFFu, n > c.cap);
     }
     if (lists) {
-        walk_list_queued<kAdjQ, kAdjBS>(active, ListSource<uint32_t>{c.list + size_t(s) * c.cap, n, s}, q,
+        walk_list_queued<kAdjQ, kAdjBS, false>(active, ListSource<uint32_t>{c.list + size_t(s) * c.cap, n, s}, q,
                                         0x7FFFFFFF, hit, body);
     } else {
         int cx, cy, cz;
         decode_key(c.key_s[s], dp.grid.dim, cx, cy, cz);
-        walk_queued<kAdjQ, kAdjBS>(active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{c.lb}, q,
+        walk_queued<kAdjQ, kAdjBS, false>(active, cx, cy, cz, neighbour_reach(dp), dp.grid.dim, LbRows{c.lb}, q,
                                    0x7FFFFFFF, hit, body);
     }
 }

@@ -225,7 +225,7 @@ __device__ __forceinline__ void walk_neighbours(int cx, int cy, int cz, int reac
 // neighbours are processed (the lambda cap: the reference stops at the first
 // `cap` neighbours in walk order).  Every lane of the warp must call this
 // (inactive lanes with active = false).
-template <int Q, int kStride, class RowRange, class Hit, class Body>
+template <int Q, int kStride, bool kCapped = true, class RowRange, class Hit, class Body>
 __device__ __forceinline__ void walk_queued(bool active, int cx, int cy, int cz, int reach, int3 dim,
                                             RowRange&& rowRange, uint32_t* q, int maxHits, Hit&& hit,
                                             Body&& body) {
@@ -264,7 +264,7 @@ __device__ __forceinline__ void walk_queued(bool active, int cx, int cy, int cz,
                 if (hit(k)) {
                     q[cnt * kStride] = k;
                     ++cnt;
-                    if (++total >= maxHits) done = true;
+                    if (kCapped && ++total >= maxHits) done = true;
                 }
                 if (!done && ++k >= e) next_row();
             }
@@ -378,7 +378,7 @@ struct ListChunk<uint16_t> {
 // has queued (all those lanes busy, two at a time so that their independent
 // arithmetic interleaves; each lane still adds its terms in order), and once
 // no list is being walked it empties the rings.
-template <int Q, int kStride, class E, class QT, class Hit, class Body>
+template <int Q, int kStride, bool kCapped = true, class E, class QT, class Hit, class Body>
 __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E>& src, QT* q, int maxHits,
                                                  Hit&& hit, Body&& body) {
     constexpr int kChunk = 8;
@@ -393,16 +393,19 @@ __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E
     if (!done) cur.load(src.lst);
     for (;;) {
         if (!done && cnt <= uint32_t(Q - kChunk)) {
+            const uint32_t left = n - e;  // > 0 while the list is being walked
 #pragma unroll
             for (int u = 0; u < kChunk; ++u) {
-                const bool v = !done && e + uint32_t(u) < n;
+                const bool v = (!kCapped || !done) && uint32_t(u) < left;
                 const uint32_t k = v ? cur.get(u) : src.fill;
                 const bool h = v && hit(k);
                 // cnt + u < Q: the slot is free (live entries are head .. head + cnt - 1)
                 q[((head + cnt) & kMask) * kStride] = QT(k);
                 cnt += h ? 1u : 0u;
-                total += h ? 1 : 0;
-                done = done || total >= maxHits;
+                if (kCapped) {
+                    total += h ? 1 : 0;
+                    done = done || total >= maxHits;
+                }
             }
             e += kChunk;
             done = done || e >= n;
@@ -440,16 +443,16 @@ struct RowSource {
     const uint32_t* __restrict__ lb;
 };
 
-template <int Q, int kStride, class QT, class Hit, class Body>
+template <int Q, int kStride, bool kCapped = true, class QT, class Hit, class Body>
 __device__ __forceinline__ void walk_source(bool active, const RowSource& r, QT* q, int maxHits, Hit&& hit,
                                             Body&& body) {
     static_assert(std::is_same<QT, uint32_t>::value, "stencil walks queue 32-bit slots");
-    walk_queued<Q, kStride>(active, r.cx, r.cy, r.cz, r.reach, r.dim, LbRows{r.lb}, q, maxHits, hit, body);
+    walk_queued<Q, kStride, kCapped>(active, r.cx, r.cy, r.cz, r.reach, r.dim, LbRows{r.lb}, q, maxHits, hit, body);
 }
-template <int Q, int kStride, class E, class QT, class Hit, class Body>
+template <int Q, int kStride, bool kCapped = true, class E, class QT, class Hit, class Body>
 __device__ __forceinline__ void walk_source(bool active, const ListSource<E>& l, QT* q, int maxHits, Hit&& hit,
                                             Body&& body) {
-    walk_list_queued<Q, kStride>(active, l, q, maxHits, hit, body);
+    walk_list_queued<Q, kStride, kCapped>(active, l, q, maxHits, hit, body);
 }
 
 // Where the queued passes read a candidate's data: the cell-ordered arrays in
@@ -732,7 +735,7 @@ __device__ __forceinline__ float3 delta_queued_sum(bool active, uint32_t s, floa
     float3 dsum = make_float3(0.f, 0.f, 0.f);
     const float h2 = dp.kernel.h2;
     constexpr bool kSelf = std::is_same<Src, RowSource>::value;
-    walk_source<Q, kStride>(
+    walk_source<Q, kStride, false>(
         active, src, q, 0x7FFFFFFF,
         [&](uint32_t k) -> bool {
             float rx, ry, rz;
@@ -800,7 +803,7 @@ __device__ __forceinline__ float4 xsph_queued(bool active, uint32_t s, float4 pi
     int count = 0;
     const float h2 = dp.kernel.h2;
     constexpr bool kSelf = std::is_same<Src, RowSource>::value;
-    walk_source<Q, kStride>(
+    walk_source<Q, kStride, false>(
         active, src, q, 0x7FFFFFFF,
         [&](uint32_t k) -> bool {
             float rx, ry, rz;
