@@ -394,17 +394,23 @@ __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E
     for (;;) {
         if (!done && cnt <= uint32_t(Q - kChunk)) {
             const uint32_t left = n - e;  // > 0 while the list is being walked
+            const uint32_t before = cnt;
 #pragma unroll
             for (int u = 0; u < kChunk; ++u) {
-                const bool v = (!kCapped || !done) && uint32_t(u) < left;
+                const bool v = uint32_t(u) < left;
                 const uint32_t k = v ? cur.get(u) : src.fill;
                 const bool h = v && hit(k);
                 // cnt + u < Q: the slot is free (live entries are head .. head + cnt - 1)
                 q[((head + cnt) & kMask) * kStride] = QT(k);
                 cnt += h ? 1u : 0u;
-                if (kCapped) {
-                    total += h ? 1 : 0;
-                    done = done || total >= maxHits;
+            }
+            if (kCapped) {
+                // hits past the cap are the last ones queued: drop them
+                total += int(cnt - before);
+                if (total >= maxHits) {
+                    cnt -= uint32_t(total - maxHits);
+                    total = maxHits;
+                    done = true;
                 }
             }
             e += kChunk;

@@ -82,6 +82,28 @@ def test_step_by_step_over_a_run(gpu, lib, orc, hashed):
             s.step()
 
 
+# Boxes whose grids have 1,023, 1,024, 1,025 and 2,048 cells (the lower-bound
+# table holds numCells + 1 entries and is filled in blocks of 1,024) and 125.
+EDGE_BOXES = [(0.375, 0.03, 0.125), (0.1875, 0.0875, 0.0875), (0.5, 0.05, 0.05), (0.1875, 0.1875, 0.0875),
+              (0.05, 0.05, 0.05)]
+
+
+@pytest.mark.parametrize("box", EDGE_BOXES)
+@pytest.mark.parametrize("corner", ["min", "max"])
+def test_dense_cell_tables_at_block_edges(gpu, lib, orc, box, corner):
+    """A few particles packed in the first cells (long empty tail) or in the
+    last cells (long empty head) of grids sized around the fill's blocks."""
+    p = pbfx.dam_break_params(box, 1, 18)
+    assert pbfx.num_cells(p) in (1023, 1024, 1025, 2048, 125)
+    dims = (3, 2, 3)
+    if corner == "min":
+        origin = (0.005, 0.005, 0.005)
+    else:
+        origin = tuple(b - 0.005 - (n - 1) * 0.01 for b, n in zip(box, dims))
+    pos = pbfx.seed_lattice(lib, *dims, origin, 0.01, 0.0005, 0xC0FFEE, p)
+    compare_step(lib, orc, p, pos, np.zeros_like(pos), hashed=False)
+
+
 def test_xsph_disabled_and_restitution(gpu, lib, orc):
     p, pos, vel = c1_scene(lib)
     p.xsph_c = 0.0
