@@ -365,12 +365,57 @@ struct ListWriter {
         }
         cnt += __popc(m);
     }
+    // Staged tile with cap >= 32: a list of 16-bit entries has 2 cap of room,
+    // so while cnt <= cap (a warp-uniform test) an emit writes below cap + 32
+    // and needs no bound per lane; entries past cap are never read (the count
+    // then exceeds cap and the warp walks the stencil).
+    __device__ __forceinline__ void emit16(bool in, uint32_t k, uint32_t shift, uint32_t cap, uint32_t lt) {
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
+        if (in && cnt <= cap) reinterpret_cast<uint16_t*>(out)[cnt + __popc(m & lt)] = uint16_t(k + shift);
+        cnt += __popc(m);
+    }
 };
+
+// One row of the list build for G particles of one cell: candidates [b, e),
+// 32 per step.  kSlack: staged tile with cap >= 32 (ListWriter::emit16).
+template <int G, bool kSlack>
+__device__ __forceinline__ void build_row(const float4* __restrict__ pred, const uint32_t (&sl)[G],
+                                          const float4& p0, const unsigned long long (&px)[G / 2],
+                                          const unsigned long long (&py)[G / 2],
+                                          const unsigned long long (&pz)[G / 2], int used, uint32_t b, uint32_t e,
+                                          uint32_t shift, float R2, uint32_t cap, bool staged, uint32_t lt,
+                                          uint32_t lane, ListWriter (&w)[G]) {
+#pragma unroll 2
+    for (uint32_t c = b; c < e; c += 32u) {
+        const uint32_t k = c + lane;
+        const bool valid = k < e;
+        const float4 pj = valid ? __ldg(pred + k) : p0;
+        const unsigned long long jx = pk2(pj.x, pj.x), jy = pk2(pj.y, pj.y), jz = pk2(pj.z, pj.z);
+#pragma unroll
+        for (int h = 0; h < G / 2; ++h) {
+            // r^2 = rz^2 + (rx^2 + ry^2), as the neighbour passes compute it
+            const unsigned long long dx = sub2(px[h], jx), dy = sub2(py[h], jy), dz = sub2(pz[h], jz);
+            const float2 r2 = upk2(fma2(dz, dz, fma2(dx, dx, mul2(dy, dy))));
+            const bool in0 = valid && k != sl[2 * h] && !(r2.x > R2);
+            const bool in1 = valid && k != sl[2 * h + 1] && !(r2.y > R2);
+            if (kSlack)
+                w[2 * h].emit16(in0, k, shift, cap, lt);
+            else
+                w[2 * h].emit(in0, k, shift, cap, staged, lt);
+            if (2 * h + 1 < used) {
+                if (kSlack)
+                    w[2 * h + 1].emit16(in1, k, shift, cap, lt);
+                else
+                    w[2 * h + 1].emit(in1, k, shift, cap, staged, lt);
+            }
+        }
+    }
+}
 
 // The row walk of the list build for G particles of one cell (G even;
 // particle g emits only when g < used): each candidate is loaded once and
 // tested against the particles two at a time with packed arithmetic.
-template <int G>
+template <int G, bool kSlack>
 __device__ __forceinline__ void build_rows(const float4* __restrict__ pred, const uint32_t (&sl)[G],
                                            const float4 (&pp)[G], int used, int nrows, uint32_t rb, uint32_t re,
                                            uint32_t planShift, float R2, uint32_t cap, bool staged, uint32_t lt,
@@ -388,22 +433,7 @@ __device__ __forceinline__ void build_rows(const float4* __restrict__ pred, cons
         const uint32_t e = __shfl_sync(0xFFFFFFFFu, re, rr);
         // staged tiles have nrows <= 32, so the plan's lane rr is row rr
         const uint32_t shift = __shfl_sync(0xFFFFFFFFu, planShift, rr);
-#pragma unroll 2
-        for (uint32_t c = b; c < e; c += 32u) {
-            const uint32_t k = c + lane;
-            const bool valid = k < e;
-            const float4 pj = valid ? __ldg(pred + k) : pp[0];
-            const unsigned long long jx = pk2(pj.x, pj.x), jy = pk2(pj.y, pj.y), jz = pk2(pj.z, pj.z);
-#pragma unroll
-            for (int h = 0; h < G / 2; ++h) {
-                // r^2 = rz^2 + (rx^2 + ry^2), as the neighbour passes compute it
-                const unsigned long long dx = sub2(px[h], jx), dy = sub2(py[h], jy), dz = sub2(pz[h], jz);
-                const float2 r2 = upk2(fma2(dz, dz, fma2(dx, dx, mul2(dy, dy))));
-                w[2 * h].emit(valid && k != sl[2 * h] && !(r2.x > R2), k, shift, cap, staged, lt);
-                if (2 * h + 1 < used)
-                    w[2 * h + 1].emit(valid && k != sl[2 * h + 1] && !(r2.y > R2), k, shift, cap, staged, lt);
-            }
-        }
+        build_row<G, kSlack>(pred, sl, pp[0], px, py, pz, used, b, e, shift, R2, cap, staged, lt, lane, w);
     }
 }
 
@@ -429,6 +459,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     const uint32_t cap = lbuf.cap;
     const WarpPlan plan = plan_tile_warp<Sh>(key_s, lb, S, lbuf, s0 - s0 % uint32_t(Sh::kTile), N);
     const bool staged = plan.staged && lbuf.staging;
+    const bool slack = staged && cap >= 32u;  // ListWriter::emit16
     const uint32_t planShift = plan.base - plan.start;  // lane r: stage index of slot k in row r is k + shift
     const uint32_t lt = lanemask_lt();
     uint32_t longest = 0, overflowed = 0;
@@ -507,7 +538,10 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
                 pp[g] = pred[sl[g]];
                 w[g] = ListWriter{list + size_t(sl[g]) * cap, 0u};
             }
-            build_rows<4>(pred, sl, pp, 4, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
+            if (slack)
+                build_rows<4, true>(pred, sl, pp, 4, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
+            else
+                build_rows<4, false>(pred, sl, pp, 4, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 if (lane == 0) count[sl[g]] = w[g].cnt;
@@ -541,7 +575,10 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
             const uint32_t sl[2] = {s, sB};
             const float4 pp[2] = {pa, pb};
             ListWriter w[2] = {wa, wb};
-            build_rows<2>(pred, sl, pp, used, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
+            if (slack)
+                build_rows<2, true>(pred, sl, pp, used, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
+            else
+                build_rows<2, false>(pred, sl, pp, used, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
             wa = w[0];
             wb = w[1];
         } else {
