@@ -352,6 +352,11 @@ int pbf_destroy(pbf_sim* h) {
 
 void* pbf_stream(pbf_sim* h) { return h ? static_cast<void*>(h->sim.cudaStream()) : nullptr; }
 
+int pbf_set_stream(pbf_sim* h, void* stream) {
+    if (!h) return PBF_ERR_INVALID;
+    return h->sim.setStream(static_cast<cudaStream_t>(stream)) ? PBF_OK : PBF_ERR_CUDA;
+}
+
 int pbf_device_state(pbf_sim* h, float4** d_pos, float4** d_vel) {
     if (!h) return PBF_ERR_INVALID;
     if (d_pos) *d_pos = h->sim.devicePositionsMutable();

@@ -89,7 +89,8 @@ int3 dims_of(const sim::GridBounds& g) {
 }  // namespace pbf
 
 struct pbf_ensemble {
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // where work is enqueued: `own` or a caller's stream
+    cudaStream_t own = nullptr;     // created with the ensemble; the graph is captured here
     uint32_t N = 0, S = 0, totalCells = 0;
     int keyBits = 1, passes = 1;
     std::vector<uint32_t> offsets;
@@ -107,13 +108,14 @@ struct pbf_ensemble {
 
     ~pbf_ensemble() {
         if (stream) cudaStreamSynchronize(stream);
+        if (own && own != stream) cudaStreamSynchronize(own);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         for (void* p : {(void*)pos, (void*)vel, (void*)pred_a, (void*)pred_b, (void*)pos_s, (void*)vel_s, (void*)lam,
                         (void*)keys, (void*)key_s, (void*)perm, (void*)lb, (void*)sceneOfId, (void*)sceneOfSlot,
                         (void*)err, (void*)scenes, sortTemp, (void*)nbrList, (void*)nbrCount, (void*)nbrStats})
             if (p) cudaFree(p);
-        if (stream) cudaStreamDestroy(stream);
+        if (own) cudaStreamDestroy(own);
     }
 
     float4* final_pred() const { return (passes % 2 == 0) ? pred_a : pred_b; }
@@ -143,7 +145,7 @@ struct pbf_ensemble {
     }
 
     // The step as launches on `stream` (captured once into the graph).
-    cudaError_t enqueue() {
+    cudaError_t enqueue(cudaStream_t stream) {
         using namespace pbf;
         if (N == 0) return cudaSuccess;
         const unsigned g = blocks_for(N, kBS);
@@ -162,10 +164,10 @@ struct pbf_ensemble {
     }
 
     int capture() {
-        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBF_ERR_CUDA;
-        const cudaError_t le = enqueue();
+        if (cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBF_ERR_CUDA;
+        const cudaError_t le = enqueue(own);
         cudaGraph_t gr = nullptr;
-        const cudaError_t ce = cudaStreamEndCapture(stream, &gr);
+        const cudaError_t ce = cudaStreamEndCapture(own, &gr);
         if (le != cudaSuccess || ce != cudaSuccess || !gr) {
             if (gr) cudaGraphDestroy(gr);
             cudaGetLastError();
@@ -238,13 +240,14 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
     for (uint32_t s = 0; s < num_scenes; ++s)
         std::fill(sceneOfId.begin() + offsets[s], sceneOfId.begin() + offsets[s + 1], s);
     const uint32_t N = e->N;
-    bool ok = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) == cudaSuccess && dalloc(&e->pos, N) &&
+    bool ok = cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking) == cudaSuccess && dalloc(&e->pos, N) &&
               dalloc(&e->vel, N) && dalloc(&e->pred_a, N) && dalloc(&e->pred_b, N) && dalloc(&e->pos_s, N) &&
               dalloc(&e->vel_s, N) && dalloc(&e->lam, N) && dalloc(&e->keys, N) && dalloc(&e->key_s, N) &&
               dalloc(&e->perm, N) && dalloc(&e->lb, size_t(e->totalCells) + 1) && dalloc(&e->sceneOfId, N) &&
               dalloc(&e->sceneOfSlot, N) && dalloc(&e->err, 1) && dalloc(&e->scenes, num_scenes) &&
               cudaMalloc(&e->sortTemp, e->sortBytes) == cudaSuccess && dalloc(&e->nbrStats, 2) &&
               fused_prepare_kernels() == cudaSuccess;
+    e->stream = e->own;
     if (ok) {  // neighbour lists: optional (without them every scene walks the stencil)
         const uint32_t cap = sim::Simulator::kDefaultListCapacity;
         if (dalloc(&e->nbrList, size_t(N) * cap) && dalloc(&e->nbrCount, N)) {
@@ -285,6 +288,15 @@ int pbf_ensemble_destroy(pbf_ensemble* e) {
 }
 
 void* pbf_ensemble_stream(pbf_ensemble* e) { return e ? static_cast<void*>(e->stream) : nullptr; }
+
+int pbf_ensemble_set_stream(pbf_ensemble* e, void* stream) {
+    if (!e || !e->own) return PBF_ERR_INVALID;
+    const cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : e->own;
+    if (next == e->stream) return PBF_OK;
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess) return PBF_ERR_CUDA;
+    e->stream = next;
+    return PBF_OK;
+}
 
 uint32_t pbf_ensemble_num_particles(pbf_ensemble* e) { return e ? e->N : 0u; }
 

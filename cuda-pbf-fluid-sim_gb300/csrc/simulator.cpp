@@ -282,7 +282,8 @@ bool Simulator::initialize(const SimParams& p, bool useHashedGrid) {
     m_useHashedGrid = useHashedGrid;
     const uint32_t nc = num_cells(m_params.grid.dim);
     if (nc == 0) return false;
-    if (cudaStreamCreateWithFlags(&m_stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaStreamCreateWithFlags(&m_ownStream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    m_stream = m_ownStream;
     uint32_t cap = std::max(p.maxParticles, p.numParticles);
     if (cap == 0) cap = 1;
     if (!m_bufs.allocate(cap)) return false;
@@ -307,11 +308,13 @@ bool Simulator::initialize(const SimParams& p, bool useHashedGrid) {
 
 void Simulator::shutdown() {
     destroyGraph();
-    if (m_stream) {
-        cudaStreamSynchronize(m_stream);
-        cudaStreamDestroy(m_stream);
-        m_stream = nullptr;
+    if (m_stream) cudaStreamSynchronize(m_stream);
+    if (m_ownStream) {
+        cudaStreamSynchronize(m_ownStream);
+        cudaStreamDestroy(m_ownStream);
+        m_ownStream = nullptr;
     }
+    m_stream = nullptr;
     m_bufs.release();
     m_grid.release();
     m_paramsValid = false;
@@ -358,9 +361,9 @@ bool Simulator::ensureCapacity(uint32_t n) {
 bool Simulator::captureGraph() {
     destroyGraph();
     cudaGraph_t g = nullptr;
-    if (cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
-    m_pipeline.runFull(m_ctx, m_params, m_stream);
-    cudaError_t e = cudaStreamEndCapture(m_stream, &g);
+    if (cudaStreamBeginCapture(m_ownStream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    m_pipeline.runFull(m_ctx, m_params, m_ownStream);
+    cudaError_t e = cudaStreamEndCapture(m_ownStream, &g);
     if (e != cudaSuccess || !g) {
         cudaGetLastError();
         return false;
@@ -399,6 +402,15 @@ bool Simulator::step(const SimParams& p) {
     }
     if (cudaGraphLaunch(m_graphExec, m_stream) != cudaSuccess) return false;
     ++m_frameIndex;
+    return true;
+}
+
+bool Simulator::setStream(cudaStream_t s) {
+    if (!m_ownStream) return false;
+    const cudaStream_t next = s ? s : m_ownStream;
+    if (next == m_stream) return true;
+    if (cudaStreamSynchronize(m_stream) != cudaSuccess) return false;
+    m_stream = next;
     return true;
 }
 
@@ -500,44 +512,46 @@ int Simulator::profileStep(const SimParams& p, float* ms, const char** names, in
         {"lambda_1", "lambda_2", "lambda_3", "lambda_4", "lambda_5", "lambda_6", "lambda_7", "lambda_8"},
         {"delta_1", "delta_2", "delta_3", "delta_4", "delta_5", "delta_6", "delta_7", "delta_8"},
         {"lists_1", "lists_2", "lists_3", "lists_4", "lists_5", "lists_6", "lists_7", "lists_8"}};
+    // captured on the owned stream, launched on the current one
+    const cudaStream_t cs = m_ownStream;
     std::vector<cudaEvent_t> ev;
     std::vector<const char*> nm;
     auto mark = [&](const char* name) {
         cudaEvent_t e;
         cudaEventCreate(&e);
-        cudaEventRecordWithFlags(e, m_stream, cudaEventRecordExternal);
+        cudaEventRecordWithFlags(e, cs, cudaEventRecordExternal);
         ev.push_back(e);
         if (name) nm.push_back(name);
     };
     cudaGraph_t graph = nullptr;
-    if (cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1;
     mark(nullptr);
-    pbf::fused_predict_keys(b, sh, m_stream);
+    pbf::fused_predict_keys(b, sh, cs);
     mark("predict_keys");
-    pbf::fused_sort(b, sh, m_stream);
+    pbf::fused_sort(b, sh, cs);
     mark("sort");
-    pbf::fused_gather_and_tables(b, sh, m_stream);
+    pbf::fused_gather_and_tables(b, sh, cs);
     mark("gather_tables");
     if (sh.iters > 8) {
-        pbf::fused_solve(b, sh, m_stream);
+        pbf::fused_solve(b, sh, cs);
         mark("solve");
     } else if (sh.iters <= 0) {
-        pbf::fused_solve(b, sh, m_stream);
+        pbf::fused_solve(b, sh, cs);
         mark("finalize");
     } else {
         for (int it = 0; it < sh.iters; ++it) {
-            if (pbf::fused_build_lists(b, sh, it, m_stream) == cudaSuccess) mark(kIterNames[2][it]);
-            pbf::fused_solve_phase(b, sh, it, 0, m_stream);
+            if (pbf::fused_build_lists(b, sh, it, cs) == cudaSuccess) mark(kIterNames[2][it]);
+            pbf::fused_solve_phase(b, sh, it, 0, cs);
             mark(kIterNames[0][it]);
-            pbf::fused_solve_phase(b, sh, it, 1, m_stream);
+            pbf::fused_solve_phase(b, sh, it, 1, cs);
             mark(kIterNames[1][it]);
         }
     }
-    pbf::fused_commit(b, sh, m_stream);
+    pbf::fused_commit(b, sh, cs);
     mark("commit");
     int n = 0;
     cudaGraphExec_t exec = nullptr;
-    if (cudaStreamEndCapture(m_stream, &graph) == cudaSuccess && graph &&
+    if (cudaStreamEndCapture(cs, &graph) == cudaSuccess && graph &&
         cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess && cudaGraphLaunch(exec, m_stream) == cudaSuccess &&
         cudaStreamSynchronize(m_stream) == cudaSuccess) {
         for (size_t k = 1; k < ev.size() && n < cap; ++k, ++n) {

@@ -136,6 +136,7 @@ _SIGS = {
     "pbf_create": ([C.POINTER(SimParams), _I, C.POINTER(_VP)], _I),
     "pbf_destroy": ([_VP], _I),
     "pbf_stream": ([_VP], _VP),
+    "pbf_set_stream": ([_VP, _VP], C.c_int),
     "pbf_device_state": ([_VP, C.POINTER(_VP), C.POINTER(_VP)], _I),
     "pbf_upload_state": ([_VP, _VP, _VP], _I),
     "pbf_download_state": ([_VP, _VP, _VP], _I),
@@ -161,6 +162,7 @@ _SIGS = {
     "pbf_ensemble_create": ([C.POINTER(SimParams), _U32, C.POINTER(_VP)], _I),
     "pbf_ensemble_destroy": ([_VP], _I),
     "pbf_ensemble_stream": ([_VP], _VP),
+    "pbf_ensemble_set_stream": ([_VP, _VP], C.c_int),
     "pbf_ensemble_num_particles": ([_VP], _U32),
     "pbf_ensemble_scene_offsets": ([_VP, _VP], _I),
     "pbf_ensemble_upload_state": ([_VP, _VP, _VP], _I),
@@ -409,6 +411,10 @@ class Sim:
     def stream_ptr(self) -> int:
         return int(self.lib.pbf_stream(self.h) or 0)
 
+    def set_stream(self, stream: int | None):
+        """Enqueue on a caller's cudaStream_t (an int); None: the handle's own stream."""
+        check(self.lib.pbf_set_stream(self.h, C.c_void_p(stream or None)), "set_stream")
+
     def density_stats(self):
         out = (C.c_double * 4)()
         check(self.lib.pbf_density_stats(self.h, C.byref(out)), "density_stats")
@@ -456,6 +462,10 @@ class Ensemble:
 
     def stream_ptr(self) -> int:
         return int(self.lib.pbf_ensemble_stream(self.h) or 0)
+
+    def set_stream(self, stream: int | None):
+        """Enqueue on a caller's cudaStream_t (an int); None: the ensemble's own stream."""
+        check(self.lib.pbf_ensemble_set_stream(self.h, C.c_void_p(stream or None)), "ensemble set_stream")
 
     def launches_per_step(self) -> int:
         return int(self.lib.pbf_ensemble_launches_per_step(self.h))

@@ -202,8 +202,15 @@ enum { PBF_GRID_DENSE = 0, PBF_GRID_HASHED = 1 };
  * p->grid (dims recomputed with ComputeDims).  Owns a non-blocking stream. */
 int pbf_create(const pbf_sim_params* p, int grid_mode, pbf_sim** out);
 int pbf_destroy(pbf_sim* sim);
-/* The handle's stream (cudaStream_t). */
+/* The stream the handle enqueues its work on (cudaStream_t): its own
+ * non-blocking stream unless pbf_set_stream chose another. */
 void* pbf_stream(pbf_sim* sim);
+/* Enqueue the handle's work (steps, copies, profiling) on a caller's stream
+ * from now on, as the reference's launchers take one (sim/phases.cpp:8-25);
+ * NULL returns to the handle's own stream.  The switch waits for the work
+ * already queued on the previous stream.  The step graph is still captured
+ * on the handle's own stream and launched on the chosen one. */
+int pbf_set_stream(pbf_sim* sim, void* stream);
 /* Device pointers of the committed state (float4[N], original particle order). */
 int pbf_device_state(pbf_sim* sim, float4** d_pos, float4** d_vel);
 
@@ -306,6 +313,8 @@ typedef struct pbf_ensemble pbf_ensemble;
 int pbf_ensemble_create(const pbf_sim_params* scenes, uint32_t num_scenes, pbf_ensemble** out);
 int pbf_ensemble_destroy(pbf_ensemble* ens);
 void* pbf_ensemble_stream(pbf_ensemble* ens);
+/* As pbf_set_stream, for an ensemble. */
+int pbf_ensemble_set_stream(pbf_ensemble* ens, void* stream);
 uint32_t pbf_ensemble_num_particles(pbf_ensemble* ens);
 /* offsets: num_scenes + 1 entries. */
 int pbf_ensemble_scene_offsets(pbf_ensemble* ens, uint32_t* offsets);

@@ -75,6 +75,12 @@ public:
     // One step on the simulator's stream (asynchronous).
     bool step(const SimParams& p);
 
+    // Runs the simulator's work on a caller's stream from now on (nullptr:
+    // back to the stream the simulator owns).  The switch waits for the work
+    // already queued on the old stream.  Graphs are still captured on the
+    // owned stream and launched on the current one.
+    bool setStream(cudaStream_t s);
+
     // Accessors (original particle order).
     const float4* devicePositions() const { return m_bufs.d_pos; }
     float4* renderPositionPtr() const { return m_bufs.d_pos; }
@@ -148,7 +154,8 @@ private:
     DeviceBuffers m_bufs{};
     GridBuffers m_grid{};
     bool m_useHashedGrid = true;
-    cudaStream_t m_stream = nullptr;
+    cudaStream_t m_stream = nullptr;     // where work is enqueued (owned or a caller's)
+    cudaStream_t m_ownStream = nullptr;  // created by initialize; graphs are captured here
     cudaGraph_t m_graph = nullptr;
     cudaGraphExec_t m_graphExec = nullptr;
     bool m_graphDirty = true;

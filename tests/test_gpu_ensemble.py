@@ -93,3 +93,29 @@ def test_ensemble_scene_generator_is_seeded(lib):
         assert all(0.3 <= e <= 1.0 + 1e-6 for e in ext)
         g = np.array([s.gravity.x, s.gravity.y, s.gravity.z])
         assert abs(np.linalg.norm(g) - 9.8) < 1e-4 and -g[1] / 9.8 >= np.cos(np.radians(15.0)) - 1e-6
+
+
+@pytest.mark.gpu
+def test_ensemble_caller_stream(gpu, lib):
+    """pbf_ensemble_set_stream: the same state on a caller's stream."""
+    torch = pytest.importorskip("torch")
+    scenes, pos = mixed_scenes(lib)
+    vel = np.zeros_like(pos)
+    with pbfx.Ensemble(lib, scenes) as e:
+        e.upload(pos, vel)
+        e.step(8)
+        ref = e.download()
+    st = torch.cuda.Stream()
+    with pbfx.Ensemble(lib, scenes) as e:
+        own = e.stream_ptr()
+        e.set_stream(st.cuda_stream)
+        assert e.stream_ptr() == st.cuda_stream != own
+        e.upload(pos, vel)
+        pbfx.check(lib.pbf_ensemble_step(e.h, 5), "ensemble step")  # asynchronous, on st
+        st.synchronize()
+        e.set_stream(None)
+        assert e.stream_ptr() == own
+        e.step(3)
+        got = e.download()
+    np.testing.assert_array_equal(got[0], ref[0])
+    np.testing.assert_array_equal(got[1], ref[1])

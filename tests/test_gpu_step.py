@@ -222,3 +222,32 @@ def test_nonfinite_state_is_reported(gpu, lib, hashed):
         s.upload(pos, vel)
         assert lib.pbf_step_n(s.h, None, 2) == pbfx.PBF_OK
         assert lib.pbf_synchronize(s.h) == pbfx.PBF_OK
+
+
+def test_caller_stream(gpu, lib):
+    """pbf_set_stream: steps enqueued on a caller's stream give the same state;
+    NULL returns to the handle's own stream."""
+    torch = pytest.importorskip("torch")
+    p, pos, vel = c1_scene(lib)
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        s.upload(pos, vel)
+        s.step(6)
+        ref = s.download()
+    st = torch.cuda.Stream()
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        own = s.stream_ptr()
+        s.set_stream(st.cuda_stream)
+        assert s.stream_ptr() == st.cuda_stream != own
+        s.upload(pos, vel)
+        for _ in range(5):
+            pbfx.check(lib.pbf_step(s.h, None), "step")  # asynchronous, on st
+        done = torch.cuda.Event()
+        done.record(st)
+        done.synchronize()
+        assert st.query()
+        s.set_stream(None)
+        assert s.stream_ptr() == own
+        s.step(1)
+        got = s.download()
+    np.testing.assert_array_equal(got[0], ref[0])
+    np.testing.assert_array_equal(got[1], ref[1])
