@@ -262,6 +262,77 @@ def cpu_rate(orc, p, hashed, pos, vel, budget_s: float, max_steps: int):
     return n * steps / dt, steps, dt
 
 
+def launcher_path(lib, p, pos0, hashed: bool, warmup: int, steps: int):
+    """The step through the reference-layout phase launchers (pbf_launch_*,
+    include/pbf/pbf.h), in the reference's phase order (sim/phases.cpp:30-117,
+    sim/post_ops.cpp:25-85): what a reference build linked against this
+    library runs.  Returns (device ms per step, final positions)."""
+    import torch
+
+    import pbfx
+
+    n = pos0.shape[0]
+    nc = pbfx.num_cells(p)
+    dp = pbfx.device_params(p)
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    f4 = lambda: torch.empty((n, 4), dtype=torch.float32, device="cuda")  # noqa: E731
+    u32 = lambda k: torch.empty(max(k, 1), dtype=torch.int32, device="cuda")  # noqa: E731
+    pos, pred, delta, vel_old = torch.from_numpy(pos0).cuda(), f4(), f4(), f4()
+    vel = torch.zeros_like(pos)
+    lam = torch.empty(n, dtype=torch.float32, device="cuda")
+    keys, idx, ks, ids = u32(n), u32(n), u32(n), u32(n)
+    uk, off, cnt, st, en = u32(n), u32(n + 1), u32(1), u32(nc), u32(nc)
+    tb, sb = C.c_size_t(), C.c_size_t()
+    pbfx.check(lib.pbf_sort_pairs_query(C.byref(tb), n), "sort query")
+    pbfx.check(lib.pbf_cell_compact_scratch_query(C.byref(sb), n), "compact scratch query")
+    sort_tmp = torch.empty(max(tb.value, 1), dtype=torch.uint8, device="cuda")
+    scratch = torch.empty(max(sb.value, 1), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    S = C.c_void_p(stream.cuda_stream)
+    inv_dt = C.c_float(np.float32(1.0) / np.float32(p.dt))
+    if hashed:
+        tab = (P(uk), P(off), P(cnt))
+        lam_fn, delta_fn, xsph_fn = lib.pbf_launch_lambda_compact, lib.pbf_launch_delta_apply_compact, \
+            lib.pbf_launch_xsph_compact
+    else:
+        tab = (P(st), P(en))
+        lam_fn, delta_fn, xsph_fn = lib.pbf_launch_lambda, lib.pbf_launch_delta_apply, lib.pbf_launch_xsph
+
+    def step(cur, nxt):
+        ck = pbfx.check
+        ck(lib.pbf_launch_integrate_pred(P(cur), P(vel), P(nxt), p.gravity, C.c_float(p.dt), n, S))
+        ck(lib.pbf_launch_boundary(P(nxt), P(vel), C.byref(p.grid), C.c_float(0.0), n, S))
+        ck(lib.pbf_launch_hash_keys(P(keys), P(idx), P(nxt), C.byref(p.grid), n, S))
+        ck(lib.pbf_launch_sort_pairs(P(sort_tmp), tb.value, P(keys), P(ks), P(idx), P(ids), n, S))
+        if hashed:
+            ck(lib.pbf_launch_cell_ranges_compact(P(scratch), sb.value, P(uk), P(off), P(cnt), P(ks), n, S))
+        else:
+            ck(lib.pbf_launch_cell_ranges(P(st), P(en), P(ks), n, nc, S))
+        for _ in range(p.solverIters):
+            ck(lam_fn(P(lam), P(nxt), P(ids), P(ks), *tab, C.byref(dp), n, S))
+            ck(delta_fn(P(nxt), P(delta), P(lam), P(ids), P(ks), *tab, C.byref(dp), n, S))
+        ck(lib.pbf_launch_boundary(P(nxt), P(vel), C.byref(p.grid), C.c_float(0.0), n, S))
+        ck(lib.pbf_launch_velocity(P(vel), P(cur), P(nxt), inv_dt, n, S))
+        if p.xsph_c > 0.0:
+            with torch.cuda.stream(stream):
+                vel_old.copy_(vel)
+            ck(xsph_fn(P(vel), P(vel_old), P(nxt), P(ids), P(ks), *tab, C.byref(dp), n, S))
+        ck(lib.pbf_launch_boundary(P(nxt), P(vel), C.byref(p.grid), C.c_float(p.boundaryRestitution), n, S))
+
+    torch.cuda.synchronize()
+    for _ in range(warmup):
+        step(pos, pred)
+        pos, pred = pred, pos
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(stream)
+        step(pos, pred)
+        ev[k][1].record(stream)
+        pos, pred = pred, pos
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / steps, pos.cpu().numpy()
+
+
 def run_reference(args, cfg, world, rank):
     if rank != 0:
         return 0
@@ -447,6 +518,13 @@ def run_ours(args, cfg, world, rank, local):
                     "value": n / (ms.value * 1e-3), "unit": UNIT, "ms_per_step": ms.value,
                     "what": "reference kernels (sim/*.cu) built for sm_103a, same steps, graph per step, "
                             "no L2 flush between steps", "speedup": value / (n / (ms.value * 1e-3))}
+                # the same steps through this library's reference-layout phase launchers
+                lms, lpos = launcher_path(lib, p, pos, hashed, args.warmup, args.steps)
+                line["launcher_path"] = {
+                    "value": n / (lms * 1e-3), "unit": UNIT, "ms_per_step": lms,
+                    "what": "pbf_launch_* in the reference's phase order, one launch at a time, same steps, "
+                            "no L2 flush between steps", "speedup_vs_reference_kernels": ms.value / lms,
+                    "final_state_identical_to_reference_kernels": bool(np.array_equal(lpos, rpos))}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = pbfx.load_oracle()
