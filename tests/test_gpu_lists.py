@@ -72,6 +72,21 @@ def test_overflowing_lists_fall_back_to_the_stencil(gpu, lib, which):
     assert c == cap and longest > cap and overflowed > 0
 
 
+@pytest.mark.parametrize("cap", [24, 32, 40])
+def test_capacities_around_the_unbounded_emit(gpu, lib, cap):
+    """From a capacity of 32, staged tiles write their 16-bit lists without a
+    bound per lane (the list's 2 x capacity of room absorbs an emit that
+    starts within the capacity); below it, every emit is bounded.  Lists
+    overflow at these capacities, so the state must still equal the stencil
+    walk's, and the counts of the other lists must not be disturbed."""
+    p, pos, vel = scene(lib)
+    walk = run(lib, p, pos, vel, True, 0, 30)
+    lists = run(lib, p, pos, vel, True, cap, 30)
+    assert_same(lists, walk)
+    c, longest, overflowed = lists[3]
+    assert c == cap and longest > cap and overflowed > 0
+
+
 @pytest.mark.parametrize("iters, clamp, builds", [(3, 0.0, 1), (3, 0.02, 1), (6, 0.05, 2), (7, 0.05, 3),
                                                   (3, 0.1, 2), (4, 0.12, 2)])
 def test_list_schedule_follows_the_displacement_clamp(gpu, lib, iters, clamp, builds):
