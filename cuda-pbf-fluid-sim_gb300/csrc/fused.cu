@@ -181,18 +181,30 @@ __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uin
     WarpPlan w;
     w.nrows = side * side;
     w.lists = scene_lists(v, lbuf);
-    // sorted keys: equal (y, z) at both ends means one row for the whole tile
-    const bool single = oneScene && yf == yl && zf == zl && w.nrows <= kPlanRows;
+    // Tiles within one z-plane: lane r stages stencil offset r = (dz, dy) as
+    // the cells from (y0 + dy, x0 - reach) to (y1 + dy, x1 + reach) of plane
+    // z + dz, consecutive in sorted order, where (x0, y0) and (x1, y1) are the
+    // first and last particles' cells.  Every particle of the tile finds its
+    // row (dz, dy) inside: for a one-row tile (y0 = y1) the range is that row
+    // over the tile's x-extent, for a tile across rows it runs from the first
+    // row's tail over any whole rows to the last row's head.
+    const bool samePlane = oneScene && zf == zl && w.nrows <= kPlanRows;
     w.start = 0;
     w.len = 0;
-    if (single && lane < w.nrows) {
+    if (samePlane && lane < w.nrows) {
         const int z = zf + lane / side - reach;
-        const int y = yf + lane % side - reach;
-        if (z >= 0 && z < dim.z && y >= 0 && y < dim.y) {
+        const int dy = lane % side - reach;
+        const int ya = yf + dy, yb = yl + dy;
+        if (z >= 0 && z < dim.z && yb >= 0 && ya < dim.y) {
             const uint32_t* slb = lb + v.cellOffset;
-            const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
-            w.start = __ldg(slb + row + uint32_t(max(xf - reach, 0)));
-            w.len = __ldg(slb + row + uint32_t(min(xl + reach, dim.x - 1)) + 1u) - w.start;
+            const uint32_t plane = uint32_t(z * dim.y);
+            const uint32_t first = ya >= 0 ? (plane + uint32_t(ya)) * uint32_t(dim.x) + uint32_t(max(xf - reach, 0))
+                                           : plane * uint32_t(dim.x);
+            const uint32_t last = yb < dim.y
+                                      ? (plane + uint32_t(yb)) * uint32_t(dim.x) + uint32_t(min(xl + reach, dim.x - 1))
+                                      : (plane + uint32_t(dim.y)) * uint32_t(dim.x) - 1u;
+            w.start = __ldg(slb + first);
+            w.len = __ldg(slb + last + 1u) - w.start;
         }
     }
     uint32_t incl = w.len;
@@ -203,7 +215,7 @@ __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uin
     }
     w.total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     w.base = incl - w.len;
-    w.staged = single && w.total <= uint32_t(Sh::kStageMax);
+    w.staged = samePlane && w.total <= uint32_t(Sh::kStageMax);
     return w;
 }
 
