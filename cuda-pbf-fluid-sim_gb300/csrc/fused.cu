@@ -100,13 +100,14 @@ __device__ __forceinline__ bool scene_lists(const SceneView& v, const ListBufs& 
 
 // ------------------------------------------------------------- tiles
 // The list passes work on tiles of Sh::kTile consecutive sorted slots, one CTA
-// per tile.  When the tile's particles all lie in one scene and one (y, z)
-// row of cells, the union of their stencils is (2 reach + 1)^2 rows of
-// cells, each one contiguous slot range [start, start + len) covering the
-// tile's x range widened by reach.  If those ranges hold at most
-// Sh::kStageMax slots, the tile is "staged": every list pass copies the ranges into shared
-// memory (row r at base[r]) and the lists of its particles hold 16-bit
-// indices into that copy, so neighbour reads are shared-memory gathers.
+// per tile.  When the tile's particles all lie in one scene and one z-plane,
+// each of the (2 reach + 1)^2 stencil offsets (dz, dy) is covered by one
+// contiguous slot range [start, start + len) (plan_tile_warp): for a tile in
+// one row of cells, that row shifted by (dz, dy) over the tile's x range
+// widened by reach.  If the ranges hold at most Sh::kStageMax slots, the tile
+// is "staged": every list pass copies the ranges into shared memory (range r
+// at base[r]) and the lists of its particles hold 16-bit indices into that
+// copy, so neighbour reads are shared-memory gathers.
 // Other tiles' lists hold 32-bit sorted slots read from global memory.  The
 // plan depends only on the sorted keys, the lower-bound table and the
 // scenes, so the list builder and every list pass derive the same one.
