@@ -1,0 +1,57 @@
+"""bench.py's reference arm on CPU (no GPU needed): the JSON line's contract
+keys on the 32,768-particle case, the 'unavailable' lines of the workloads the
+reference has no counterpart for, and the rank rule (rank 0 alone prints)."""
+import contextlib
+import io
+import json
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+def run_main(argv):
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out):
+        rc = bench.main(argv)
+    lines = [ln for ln in out.getvalue().splitlines() if ln.startswith("{")]
+    return rc, lines
+
+
+def test_reference_arm_line():
+    rc, lines = run_main(["--impl", "reference", "--config", "c1", "--steps", "2", "--warmup", "3"])
+    assert rc == 0 and len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "impl", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["particles"] == 32768
+
+
+@pytest.mark.parametrize("config", ["c4", "c5"])
+def test_reference_arm_unavailable(config):
+    rc, lines = run_main(["--impl", "reference", "--config", config, "--steps", "1", "--warmup", "3"])
+    assert rc == 0 and len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unavailable"]
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    args = bench.argparse.Namespace(steps=1, warmup=3, ref_budget=1.0)
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out):
+        assert bench.run_reference(args, bench.CONFIGS["c1"], 2, 1) == 0
+    assert out.getvalue() == ""
+
+
+def test_warmup_floor():
+    with pytest.raises(SystemExit):
+        bench.main(["--warmup", "2"])
