@@ -377,7 +377,9 @@ struct ListChunk<uint16_t> {
 // after each round the warp runs as many bodies as every lane with work left
 // has queued (all those lanes busy, two at a time so that their independent
 // arithmetic interleaves; each lane still adds its terms in order), and once
-// no list is being walked it empties the rings.
+// no list is being walked it empties the rings.  kCapped: at most maxHits
+// bodies per lane (the reference's neighbour cap), applied once per chunk by
+// dropping the hits queued past it; without it no hit count is kept.
 template <int Q, int kStride, bool kCapped = true, class E, class QT, class Hit, class Body>
 __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E>& src, QT* q, int maxHits,
                                                  Hit&& hit, Body&& body) {
