@@ -223,13 +223,22 @@ def barrier(world):
         dist.barrier()
 
 
-def scene(lib, cfg):
+def scene(lib, cfg, orc=None):
+    """(params, pos, vel) of a configuration.  With orc given, the oracle's
+    restatement of the scene generation is used instead of the library's
+    (the CPU reference arm loads no product code); both give the same bits."""
     import pbfx
 
+    if orc is not None:
+        params_of = lambda box, iters, n: pbfx.oracle_dam_break_params(orc, box, iters, n)  # noqa: E731
+        lattice = lambda *a: pbfx.oracle_seed_lattice(orc, *a)  # noqa: E731
+    else:
+        params_of = pbfx.dam_break_params
+        lattice = lambda *a: pbfx.seed_lattice(lib, *a)  # noqa: E731
     nx, ny, nz = cfg["lattice"]
     n = nx * ny * nz
-    p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
-    pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
+    p = params_of(cfg["box"], cfg["iters"], n)
+    pos = lattice(nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
     if "drop" in cfg:
         # a second block, its bottom `gap` above the first block's top, at a
         # seeded (x, z) inside the box
@@ -238,11 +247,21 @@ def scene(lib, cfg):
         ox = 0.005 + rng.uniform(0.0, cfg["box"][0] - 0.01 * bx - 0.01)
         oz = 0.005 + rng.uniform(0.0, cfg["box"][2] - 0.01 * bz - 0.01)
         oy = 0.005 + 0.01 * ny + gap
-        q = pbfx.dam_break_params(cfg["box"], cfg["iters"], n + bx * by * bz)
-        pos2 = pbfx.seed_lattice(lib, bx, by, bz, (ox, oy, oz), 0.01, 0.0005, 0xC0FFEE + 1, q)
+        q = params_of(cfg["box"], cfg["iters"], n + bx * by * bz)
+        pos2 = lattice(bx, by, bz, (ox, oy, oz), 0.01, 0.0005, 0xC0FFEE + 1, q)
         pos = np.ascontiguousarray(np.concatenate([pos, pos2]))
         p = q
     return p, pos, np.zeros_like(pos)
+
+
+def config_record(cfg, n: int, nc: int, world: int, args) -> dict:
+    """The line's config object, shared by both arms so that they describe
+    the same workload in the same words."""
+    return {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"], "cells": nc,
+            "grid": "hashed" if cfg["hashed"] else "dense", "parallelism": "replicas" if world > 1 else "single",
+            "timed_steps": "steps %d..%d of the run from the seeded lattice" % (args.warmup,
+                                                                              args.warmup + args.steps - 1),
+            "l2": "flushed before every timed step (256 MiB write, untimed)"}
 
 
 def cpu_rate(orc, p, hashed, pos, vel, budget_s: float, max_steps: int):
@@ -339,10 +358,9 @@ def run_reference(args, cfg, world, rank):
     import __graft_entry__ as g
     import pbfx
 
-    g.build_library()
-    g.build_oracle()
-    lib, orc = pbfx.load(), pbfx.load_oracle()
-    p, pos, vel = scene(lib, cfg)
+    g.build_oracle()  # the CPU restatement only: this arm loads no product library
+    orc = pbfx.load_oracle()
+    p, pos, vel = scene(None, cfg, orc=orc)
     n = pos.shape[0]
     cores = orc.oracle_num_threads()
     for _ in range(args.warmup):
@@ -354,16 +372,104 @@ def run_reference(args, cfg, world, rank):
         "metric": cfg.get("metric", METRIC), "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": world,
         "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
-        "config": {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"],
-                   "grid": "hashed" if cfg["hashed"] else "dense", "implementation": "CPU restatement of the "
-                   "reference kernels (oracle/pbf_oracle.cpp), OpenMP over particles; the reference has no CPU "
-                   "PBF path"},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice, mt19937_64 0xC0FFEE)",
+        "config": config_record(cfg, n, pbfx.num_cells(p), world, args),
+        "implementation": "CPU restatement of the reference kernels (oracle/pbf_oracle.cpp), OpenMP over "
+                          "particles; the reference has no CPU PBF path",
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def read_traffic(cfg, args):
+    """The committed ncu figures of one step of the default C2 window:
+    {"step": absolute step index, "phases": {phase: (DRAM bytes, warp
+    instructions)}}, or None for other workloads."""
+    tfile = os.path.join(ROOT, "profiles", "c2_dram_traffic.txt")
+    if cfg is not CONFIGS["c2"] or not os.path.exists(tfile):
+        return None
+    step, phases = None, {}
+    for ln in open(tfile):
+        f = ln.split()
+        if not f:
+            continue
+        if f[0] == "#":
+            if len(f) >= 3 and f[1] == "step:":
+                step = int(f[2])
+            continue
+        phases[f[0]] = (int(f[1]), int(f[2]))
+    return {"step": step, "phases": phases} if step is not None and phases else None
+
+
+def density_error_report(lib, orc, sim, p, hashed, pos, vel):
+    """Density-constraint error of the state after the timed steps: the
+    library's statistics (pbf_density_stats: mean |C|, max |C|, mean max(C,0),
+    mean neighbours; C = rho/rho0 - 1) against the FP64 oracle's evaluation of
+    the same positions, and one more step taken by the library (FP32) and by
+    the FP64 oracle from that state, each scored in FP64."""
+    import pbfx
+
+    names = ("mean_abs_C", "max_abs_C", "mean_pos_C", "mean_neighbours")
+    n = pos.shape[0]
+    gpu = sim.density_stats()
+    ev = (C.c_double * 4)()
+    orc.oracle_density_stats_f32pos(C.byref(p), pbfx.ptr(pos), n, C.byref(ev))
+    # one step each: FP32 library, FP64 oracle
+    sim.step()
+    g1, _ = sim.download()
+    s32 = (C.c_double * 4)()
+    orc.oracle_density_stats_f32pos(C.byref(p), pbfx.ptr(g1), n, C.byref(s32))
+    p64 = np.ascontiguousarray(pos, dtype=np.float64)
+    v64 = np.ascontiguousarray(vel, dtype=np.float64)
+    t0 = time.perf_counter()
+    if orc.oracle_step_f64(C.byref(p), 1 if hashed else 0, pbfx.ptr(p64), pbfx.ptr(v64), n) != 0:
+        return None
+    t64 = time.perf_counter() - t0
+    s64 = (C.c_double * 4)()
+    orc.oracle_density_stats_f64pos(C.byref(p), pbfx.ptr(p64), n, C.byref(s64))
+    return {
+        "state": "after the timed steps",
+        "library_fp32": dict(zip(names, list(gpu))),
+        "fp64_oracle_same_positions": dict(zip(names, list(ev))),
+        "stats_abs_diff_mean_abs_C": abs(gpu[0] - ev[0]),
+        "next_step": {"library_fp32": dict(zip(names, list(s32))), "fp64_oracle": dict(zip(names, list(s64))),
+                      "abs_diff_mean_abs_C": abs(s32[0] - s64[0]), "fp64_oracle_seconds": t64},
+    }
+
+
+def ensemble_density_error(ens, scenes, orc, sample: int = 8):
+    """Density error of the ensemble against FP64, on every (S / sample)-th
+    scene: from the state after the timed steps, one ensemble step (FP32) and
+    one FP64 oracle step of the scene, each scored in FP64 (mean |C| with
+    C = rho/rho0 - 1).  The ensemble is left one step further on."""
+    import pbfx
+
+    pos, vel = ens.download()
+    ens.step(1)
+    g1, _ = ens.download()
+    off = ens.offsets.astype(np.int64)
+    picks = list(range(0, len(scenes), max(1, len(scenes) // sample)))[:sample]
+    rows = []
+    for k in picks:
+        p = scenes[k]
+        a, b = off[k], off[k + 1]
+        n = int(b - a)
+        s32 = (C.c_double * 4)()
+        orc.oracle_density_stats_f32pos(C.byref(p), pbfx.ptr(np.ascontiguousarray(g1[a:b])), n, C.byref(s32))
+        p64 = np.ascontiguousarray(pos[a:b], dtype=np.float64)
+        v64 = np.ascontiguousarray(vel[a:b], dtype=np.float64)
+        if orc.oracle_step_f64(C.byref(p), 1, pbfx.ptr(p64), pbfx.ptr(v64), n) != 0:
+            return None
+        s64 = (C.c_double * 4)()
+        orc.oracle_density_stats_f64pos(C.byref(p), pbfx.ptr(p64), n, C.byref(s64))
+        rows.append({"scene": k, "particles": n, "fp32_mean_abs_C": s32[0], "fp64_mean_abs_C": s64[0],
+                     "abs_diff": abs(s32[0] - s64[0])})
+    return {"state": "one step after the timed steps", "scenes": rows,
+            "max_abs_diff_mean_abs_C": max(r["abs_diff"] for r in rows),
+            "what": "ensemble step (FP32, GPU) vs FP64 oracle step of the same scene from the same state, both "
+                    "scored in FP64"}
 
 
 def e2e_step_count(args) -> int:
@@ -432,25 +538,37 @@ def run_ours(args, cfg, world, rank, local):
     total_s, units = aggregate(local_s, float(n) * args.steps, world)
     value = units / total_s
 
-    # Live per-phase profile (after the timed region): dominant kernel.
-    prof = {}
-    for _ in range(max(1, args.profile_steps)):
-        for name, ms in sim.profile_step():
+    final_pos, final_vel = sim.download()  # state after the timed steps
+    dens = density_error_report(lib, pbfx.load_oracle(), sim, p, hashed, final_pos, final_vel) \
+        if rank == 0 and world == 1 and not args.no_cpu_baseline else None
+
+    # Live per-phase profile over the timed window: the state is put back to
+    # the window's first step and each of its steps is run once more with an
+    # event between phases, so every figure below describes the timed steps.
+    sim.upload(snap_pos, snap_vel)
+    prof, per_step = {}, []
+    for _ in range(args.steps):
+        row = sim.profile_step()
+        per_step.append(dict(row))
+        for name, ms in row:
             prof.setdefault(name, []).append(ms)
+    prof_pos, _ = sim.download()
     avg = {k: sum(v) / len(v) for k, v in prof.items()}
     total_phase = sum(avg.values())
     dom = max(avg, key=avg.get)
     dom_bytes = alg_bytes_per_particle(dom, n, nc, hashed, cfg["iters"]) * n
     achieved = dom_bytes / (avg[dom] * 1e-3) / 1e9
-    # DRAM traffic and warp instructions per launch of the dominant kernel, from
-    # the committed ncu capture of the same workload.
+    # DRAM traffic and warp instructions per launch, from the committed ncu
+    # capture of one step of the same window (profiles/c2_dram_traffic.txt).
+    cap = read_traffic(cfg, args)
     traffic = inst = None
-    tfile = os.path.join(ROOT, "profiles", "c2_dram_traffic.txt")
-    if cfg is CONFIGS["c2"] and os.path.exists(tfile):
-        rows = {ln.split()[0]: ln.split()[1:] for ln in open(tfile) if ln.strip() and not ln.startswith("#")}
-        rec = rows.get(dom.split("_")[0])
+    step_traffic = None
+    if cap is not None:
+        rec = cap["phases"].get(dom)
         if rec:
-            traffic, inst = int(rec[0]), int(rec[1])
+            traffic, inst = rec
+        if set(avg) <= set(cap["phases"]):
+            step_traffic = sum(v[0] for v in cap["phases"].values())
 
     # End to end through host buffers, from the state the timed region started
     # from (the cost per step changes as the fluid settles).
@@ -463,38 +581,51 @@ def run_ours(args, cfg, world, rank, local):
         pbfx.check(lib.pbf_step_host(sim.h, pp, C.c_void_p(hp.data_ptr()), C.c_void_p(hv.data_ptr())))
     e2e_s = time.perf_counter() - t0
     e2e_total, e2e_units = aggregate(e2e_s, float(n) * e2e_steps, world)
+    e2e_pos, _ = sim.download()
     launches = sim.launches_per_step() * args.steps
     list_cap, list_longest, list_overflowed = sim.list_stats()
     sim.close()
+    cap_step = cap["step"] if cap else None
+    cap_k = (cap_step - args.warmup) if cap_step is not None else None
+    issue = None
+    if inst is not None and cap_k is not None and 0 <= cap_k < args.steps and dom in per_step[cap_k]:
+        t_cap = per_step[cap_k][dom]
+        issue = {"kernel": dom, "step": cap_step, "unit": "warp-instructions/s",
+                 "warp_instructions_per_launch": inst, "ms_at_step": t_cap,
+                 "achieved": inst / (t_cap * 1e-3), "peak": issue_peak(clk),
+                 "frac": inst / (t_cap * 1e-3) / issue_peak(clk),
+                 "note": "the neighbour passes are bound by instruction issue, not HBM: instructions of the launch "
+                         "at this step (ncu, profiles/c2_dram_traffic.txt) over the live time of the same step's "
+                         "launch; peak = 4 warp-instructions per cycle per SM x SMs x sampled SM clock"}
 
     line = {
         "metric": cfg.get("metric", METRIC), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded jittered lattice, mt19937_64 0xC0FFEE)",
-        "config": {"workload": cfg["workload"], "particles": n, "solver_iters": cfg["iters"], "cells": nc,
-                   "grid": "hashed" if hashed else "dense", "parallelism": "replicas" if world > 1 else "single",
-                   "timed_steps": "steps %d..%d of the run from the seeded lattice" % (args.warmup,
-                                                                                     args.warmup + args.steps - 1),
-                   "l2": "flushed before every timed step (256 MiB write, untimed)"},
+        "config": config_record(cfg, n, nc, world, args),
         "e2e": {"value": e2e_units / e2e_total, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
-                "steps": e2e_steps, "api": "pbf_step_host (pinned host pos/vel in, one step, pos/vel out)"},
+                "steps": e2e_steps, "api": "pbf_step_host (pinned host pos/vel in, one step, pos/vel out)",
+                "final_state_identical_to_timed_run": bool(e2e_steps == args.steps and
+                                                           np.array_equal(e2e_pos, final_pos))},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "traffic_step": cap_step,
                      "alg_bytes_per_launch": dom_bytes, "ms_per_launch": avg[dom],
-                     "share_of_step": avg[dom] / total_phase},
-        "issue_roofline": None if inst is None else {
-            "kernel": dom, "unit": "warp-instructions/s", "warp_instructions_per_launch": inst,
-            "achieved": inst / (avg[dom] * 1e-3), "peak": issue_peak(clk),
-            "frac": inst / (avg[dom] * 1e-3) / issue_peak(clk),
-            "note": "the neighbour passes are bound by FP32 issue, not HBM: instructions per launch from "
-                    "profiles/c2_dram_traffic.txt (ncu), time live; peak = 4 warp-instructions per cycle "
-                    "per SM x SMs x sampled SM clock"},
+                     "share_of_step": avg[dom] / total_phase,
+                     "window": "phase times averaged over the timed steps, replayed with events between phases"},
+        "issue_roofline": issue,
         "step_roofline": {"alg_bytes_per_particle_step": step_alg_bytes(nc, cfg["iters"]),
                           "achieved": value * step_alg_bytes(nc, cfg["iters"]) / 1e9, "peak": hbm_peak,
                           "unit": "GB/s",
-                          "frac": value * step_alg_bytes(nc, cfg["iters"]) / 1e9 / hbm_peak},
+                          "frac": value * step_alg_bytes(nc, cfg["iters"]) / 1e9 / hbm_peak,
+                          "dram_bytes_per_step": step_traffic, "dram_step": cap_step,
+                          "dram_over_alg": None if step_traffic is None else
+                          step_traffic / (step_alg_bytes(nc, cfg["iters"]) * n)},
         "phase_ms": {k: round(v, 5) for k, v in avg.items()},
+        "phase_sum_ms": round(total_phase, 5),
+        "profiled_window_identical_to_timed_run": bool(np.array_equal(prof_pos, final_pos)),
+        "density_error": dens,
         "step_ms": {"first": round(step_ms[0], 4), "median": round(statistics.median(step_ms), 4),
                     "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
         "gpu_launches": launches,
@@ -514,10 +645,16 @@ def run_ours(args, cfg, world, rank, local):
             rc = ref.ref_time_steps(pp, 1 if hashed else 0, pbfx.ptr(rpos), pbfx.ptr(rvel), n, args.warmup, args.steps,
                                     C.byref(ms))
             if rc == 0:
+                same = bool(np.array_equal(final_pos, rpos) and np.array_equal(final_vel, rvel))
                 line["reference_gpu"] = {
                     "value": n / (ms.value * 1e-3), "unit": UNIT, "ms_per_step": ms.value,
                     "what": "reference kernels (sim/*.cu) built for sm_103a, same steps, graph per step, "
-                            "no L2 flush between steps", "speedup": value / (n / (ms.value * 1e-3))}
+                            "no L2 flush between steps", "speedup": value / (n / (ms.value * 1e-3)),
+                    "final_state_identical_to_timed_run": same}
+                line["parity"] = {
+                    "timed_run_vs_reference_kernels": "bit-identical" if same else "DIFFERENT",
+                    "what": "positions and velocities after the warm-up and timed steps of the fused step (value) "
+                            "against the reference's own kernels run over the same steps from the same lattice"}
                 # the same steps through this library's reference-layout phase launchers
                 lms, lpos = launcher_path(lib, p, pos, hashed, args.warmup, args.steps)
                 line["launcher_path"] = {
@@ -685,6 +822,10 @@ def run_ensemble(args, cfg, world, rank, local):
     total_s, units = aggregate(sum(step_ms) / 1e3, float(S) * args.steps, world)
     value = units / total_s
 
+    dens = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        dens = ensemble_density_error(ens, scenes, pbfx.load_oracle())
+
     # End to end: host state in and out every step.
     hp = torch.from_numpy(snap_pos.copy()).pin_memory()
     hv = torch.from_numpy(snap_vel.copy()).pin_memory()
@@ -768,6 +909,7 @@ def run_ensemble(args, cfg, world, rank, local):
         "gpu_launches": launches,
         "autotune": tuned,
         "clocks": clk,
+        "density_error": dens,
     }
 
     # The reference's own kernels looped scene by scene (graph per step).

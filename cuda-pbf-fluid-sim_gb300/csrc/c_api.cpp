@@ -405,14 +405,17 @@ int pbf_step_host(pbf_sim* h, const pbf_sim_params* p, float4* hp, float4* hv) {
     if (!h || !hp || !hv) return PBF_ERR_INVALID;
     const size_t bytes = sizeof(float4) * h->sim.activeParticleCount();
     cudaStream_t s = h->sim.cudaStream();
-    cudaMemcpyAsync(h->sim.devicePositionsMutable(), hp, bytes, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(h->sim.deviceVelMutable(), hv, bytes, cudaMemcpyHostToDevice, s);
+    // a failed enqueue is reported as itself, before anything else is queued
+    cudaError_t e = cudaMemcpyAsync(h->sim.devicePositionsMutable(), hp, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->sim.deviceVelMutable(), hv, bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return from_cuda(e);
     int st = pbf_step(h, p);
     if (st != PBF_OK) return st;
-    cudaMemcpyAsync(hp, h->sim.devicePositions(), sizeof(float4) * h->sim.activeParticleCount(),
-                    cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(hv, h->sim.deviceVel(), sizeof(float4) * h->sim.activeParticleCount(), cudaMemcpyDeviceToHost, s);
-    return from_cuda(cudaStreamSynchronize(s));
+    const size_t out = sizeof(float4) * h->sim.activeParticleCount();
+    e = cudaMemcpyAsync(hp, h->sim.devicePositions(), out, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hv, h->sim.deviceVel(), out, cudaMemcpyDeviceToHost, s);
+    const cudaError_t se = cudaStreamSynchronize(s);
+    return from_cuda(e != cudaSuccess ? e : se);
 }
 
 int pbf_profile_step(pbf_sim* h, const pbf_sim_params* p, float* ms, const char** names, int cap, int* count) {

@@ -332,12 +332,14 @@ int pbf_ensemble_step(pbf_ensemble* e, int n) {
 int pbf_ensemble_step_host(pbf_ensemble* e, float4* pos, float4* vel) {
     if (!e || !pos || !vel) return PBF_ERR_INVALID;
     const size_t bytes = sizeof(float4) * e->N;
-    cudaMemcpyAsync(e->pos, pos, bytes, cudaMemcpyHostToDevice, e->stream);
-    cudaMemcpyAsync(e->vel, vel, bytes, cudaMemcpyHostToDevice, e->stream);
-    if (cudaGraphLaunch(e->exec, e->stream) != cudaSuccess) return PBF_ERR_CUDA;
-    cudaMemcpyAsync(pos, e->pos, bytes, cudaMemcpyDeviceToHost, e->stream);
-    cudaMemcpyAsync(vel, e->vel, bytes, cudaMemcpyDeviceToHost, e->stream);
-    return pbf::from_cuda(cudaStreamSynchronize(e->stream));
+    cudaError_t ce = cudaMemcpyAsync(e->pos, pos, bytes, cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(e->vel, vel, bytes, cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(e->exec, e->stream);
+    if (ce != cudaSuccess) return pbf::from_cuda(ce);
+    ce = cudaMemcpyAsync(pos, e->pos, bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(vel, e->vel, bytes, cudaMemcpyDeviceToHost, e->stream);
+    const cudaError_t se = cudaStreamSynchronize(e->stream);
+    return pbf::from_cuda(ce != cudaSuccess ? ce : se);
 }
 
 int pbf_ensemble_synchronize(pbf_ensemble* e) {
@@ -347,7 +349,8 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
     uint32_t err = 0;
     if (cudaMemcpy(&err, e->err, sizeof(err), cudaMemcpyDeviceToHost) != cudaSuccess) return PBF_ERR_CUDA;
     if (err) {
-        cudaMemset(e->err, 0, sizeof(uint32_t));
+        // on the ensemble's stream, so the clear is ordered before its next step
+        if (cudaMemsetAsync(e->err, 0, sizeof(uint32_t), e->stream) != cudaSuccess) return PBF_ERR_CUDA;
         if (err & pbf::kErrTimeoutBits) return PBF_ERR_TIMEOUT;
         return (err & pbf::kErrNonFiniteBit) ? PBF_ERR_NONFINITE : PBF_ERR_CUDA;
     }

@@ -287,7 +287,9 @@ __device__ __forceinline__ bool plan_and_issue(TilePlan& P, const uint32_t* __re
 // w = lam[k] when lam is given; with vel given, w = vel[k].x and sv[i] =
 // (vel[k].y, vel[k].z).  A wait that gives up sets kErrStageTimeoutBit and
 // waits once more (also bounded) so that no copy is still landing when the
-// tile moves on.  CTA-uniform; every thread calls it.
+// tile moves on; if that wait gives up too, in any thread, the stage is not
+// used: the function returns false and the tile's warps walk the stencil
+// from global memory instead.  CTA-uniform; every thread calls it.
 // The delta pass stages (x, y, z, lambda): a bulk copy of the positions
 // would need a second pass over the stage for lambda once it has landed, and
 // that measured slower than loading both in one pass, as here (sp[base[r] +
@@ -308,15 +310,17 @@ __device__ __forceinline__ void stage_rows(const TilePlan& P, bool staged, const
 }
 
 template <class Sh>
-__device__ __forceinline__ void stage_finish(TilePlan& P, bool staged, const float* __restrict__ lam,
+__device__ __forceinline__ bool stage_finish(TilePlan& P, bool staged, const float* __restrict__ lam,
                                              const float4* __restrict__ vel, float4* sp, float2* sv,
                                              uint32_t* err) {
-    if (!staged) return;
-    if (!mbar_wait_bounded(&P.bar, 0u, kSpinLimit)) {
+    if (!staged) return true;
+    bool landed = mbar_wait_bounded(&P.bar, 0u, kSpinLimit);
+    if (!landed) {
         if (err) atomicOr(err, kErrStageTimeoutBit);
-        mbar_wait_bounded(&P.bar, 0u, kSpinLimit);
+        landed = mbar_wait_bounded(&P.bar, 0u, kSpinLimit);
     }
-    if (!lam && !vel) return;
+    if (__syncthreads_or(!landed)) return false;
+    if (!lam && !vel) return true;
     for (int r = 0; r < P.nrows; ++r) {
         const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
         for (uint32_t i = threadIdx.x; i < len; i += Sh::kTile) {
@@ -330,6 +334,7 @@ __device__ __forceinline__ void stage_finish(TilePlan& P, bool staged, const flo
         }
     }
     __syncthreads();
+    return true;
 }
 
 // Packed two-lane FP32 arithmetic (Blackwell f32x2): the list test of two
@@ -665,10 +670,10 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
     const float4 pi = pred[sc];
     const GlobalData g{pred, nullptr, nullptr};
-    stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
+    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
     uint32_t n;
     LambdaAcc a;
-    if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+    if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
@@ -806,7 +811,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
         float2* sv = reinterpret_cast<float2*>(smem + Sh::kStageMax);
         const bool xs = s < N && dp.xsph_c > 0.f;  // every lane takes part in the warp-wide rounds
         const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
-        stage_finish<Sh>(P, staged, nullptr, vel_s, sp, sv, err);
+        const bool stageOk = stage_finish<Sh>(P, staged, nullptr, vel_s, sp, sv, err);
         // Queue of the queued walks: the stage area, free in tiles that are
         // not staged.  In a staged tile a warp whose lists overflowed walks
         // the stencil without a queue.
@@ -814,7 +819,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
         const GlobalData g{pred, nullptr, vel_s};
         uint32_t n;
         float4 vx = vv;
-        if (warp_lists_fit(lbuf, xs, scene_lists(v, lbuf), sc, n)) {
+        if (stageOk && warp_lists_fit(lbuf, xs, scene_lists(v, lbuf), sc, n)) {
             const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
             if (staged)
                 vx = xsph_list_inline(xs, x, vv,

@@ -127,6 +127,10 @@ constexpr int kCompactThreads = 256;
 constexpr int kCompactItems = 8;
 constexpr int kCompactTile = kCompactThreads * kCompactItems;  // 2048 slots
 
+// Values of the compaction's count word besides a count (<= N < 2^30).
+constexpr uint32_t kCountPending = 0xFEFEFEFEu;  // a byte-wise memset value
+constexpr uint32_t kCountInvalid = 0xFFFFFFFFu;
+
 struct CompactInfo {
     uint32_t tileCounter;
     uint32_t pad[63];
@@ -181,18 +185,25 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact(const uint32_t* __r
         }
         uint32_t* st = status + tile;
         uint32_t excl = 0;
+        bool gave_up = false;
         if (tile == 0) {
             st_relaxed(st, kFlagPrefix | run);
         } else {
             st_relaxed(st, kFlagAggregate | run);
-            excl = lookback_exclusive(status, tile, 1u, err);
+            excl = lookback_exclusive(status, tile, 1u, err, kSpinLimit, &gave_up);
             st_relaxed(st, kFlagPrefix | ((excl + run) & kCountMask));
         }
         s_excl = excl;
+        // The count starts as kCountPending (set before the launch).  A tile
+        // whose look-back gave up marks the table invalid with 0xFFFFFFFF; the
+        // last tile's count only replaces the pending value, so the mark
+        // survives in either order.  (excl can only fall short of the true
+        // prefix, so every index written stays below N.)
+        if (gave_up) atomicExch(count, kCountInvalid);
         if (tile == numTiles - 1u) {
             const uint32_t M = excl + run;
             off[M] = N;
-            *count = M;
+            if (!gave_up) atomicCAS(count, kCountPending, M);
         }
     }
     __syncthreads();
@@ -332,6 +343,7 @@ cudaError_t launch_compact(void* d_scratch, size_t scratch_bytes, uint32_t* uniq
     uint32_t* status = reinterpret_cast<uint32_t*>(base + compact_layout_status_off());
     if (!err) err = &info->pad[0];
     cudaError_t e = cudaMemsetAsync(base, 0, compact_layout_status_off() + size_t(tiles) * 4u, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(count, 0xFE, sizeof(uint32_t), s);  // kCountPending
     if (e != cudaSuccess) return e;
     k_compact<<<tiles, kCompactThreads, 0, s>>>(keys_sorted, N, unique_keys, offsets, count, seg, info, status, tiles,
                                                 err);

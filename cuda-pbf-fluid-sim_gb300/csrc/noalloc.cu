@@ -32,24 +32,58 @@ constexpr size_t kNoAllocScratchBytes = 256 + ((size_t((kNoAllocMaxKeys + 2047u)
 
 static __device__ __align__(256) unsigned char g_compact_scratch[kNoAllocScratchBytes];
 
-// Device address of g_compact_scratch, looked up once per device with that
-// device current (the host-side symbol is only a stand-in and must never be
-// handed to a kernel).
+// Device address of g_compact_scratch, looked up with the device current (the
+// host-side symbol is only a stand-in and must never be handed to a kernel).
+// It is cached per device together with the context it was looked up in:
+// after cudaDeviceReset the device gets a new context, the module is loaded
+// again and the array may move, so a changed context means a new lookup.  The
+// context is read through the driver entry point the runtime hands out, so
+// the library needs no link against the driver library.
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchSlot {
+    void* ctx = nullptr;
+    void* addr = nullptr;
+};
+ScratchSlot g_scratch[kMaxDevices];
+
+using CtxGetCurrentFn = int (*)(void**);  // CUresult cuCtxGetCurrent(CUcontext*)
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+
+int current_context(void** ctx) {
+    if (!g_ctx_get_current) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        // cuCtxGetCurrent has had one signature since CUDA 4.0
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return PBF_ERR_CUDA;
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+    }
+    *ctx = nullptr;
+    return g_ctx_get_current(ctx) == 0 ? PBF_OK : PBF_ERR_CUDA;  // null: no context current yet
+}
 
 int scratch_address(void** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PBF_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
+    void* ctx = nullptr;
+    int st = current_context(&ctx);
+    if (st != PBF_OK) return st;
+    ScratchSlot& slot = g_scratch[dev];
+    if (!ctx || !slot.addr || slot.ctx != ctx) {
+        // the lookup also makes the device's primary context current (and
+        // loads this library's module in it) if that has not happened yet
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_compact_scratch);
         if (e != cudaSuccess || p == nullptr) return PBF_ERR_CUDA;
-        g_scratch_addr[dev] = p;
+        st = current_context(&ctx);
+        if (st != PBF_OK || !ctx) return PBF_ERR_CUDA;
+        slot.ctx = ctx;
+        slot.addr = p;
     }
-    *out = g_scratch_addr[dev];
+    *out = slot.addr;
     return PBF_OK;
 }
 

@@ -109,9 +109,10 @@ constexpr uint32_t kCountMask = (1u << 30) - 1u;
 
 // Walks back over tile statuses [tile-1, tile-2, ...] until an inclusive
 // prefix is found; returns the exclusive prefix of `tile`.  Every poll loop is
-// bounded by kSpinLimit.
+// bounded by kSpinLimit; *gave_up (when given) is set if one ran out.
 __device__ __forceinline__ uint32_t lookback_exclusive(const uint32_t* status, uint32_t tile, uint32_t stride,
-                                                       uint32_t* err, uint32_t spin_limit = kSpinLimit) {
+                                                       uint32_t* err, uint32_t spin_limit = kSpinLimit,
+                                                       bool* gave_up = nullptr) {
     uint32_t excl = 0;
     int64_t k = int64_t(tile) - 1;
     while (k >= 0) {
@@ -121,6 +122,7 @@ __device__ __forceinline__ uint32_t lookback_exclusive(const uint32_t* status, u
         while ((v & kFlagMask) == 0u) {
             if (++spins > spin_limit) {
                 atomicOr(err, kErrLookbackTimeout);
+                if (gave_up) *gave_up = true;
                 return excl;
             }
             __nanosleep(32);
@@ -521,7 +523,7 @@ struct DenseRows {
 struct CompactRows {
     const uint32_t* __restrict__ uk;
     const uint32_t* __restrict__ off;
-    uint32_t M;
+    uint32_t M;  // the caller passes min(count, N): a timed-out table's 0xFFFFFFFF stays in bounds
     __device__ __forceinline__ uint2 operator()(uint32_t c0, uint32_t c1) const {
         uint32_t lo = 0, hi = M;
         while (lo < hi) {

@@ -67,7 +67,7 @@ __global__ void k_lambda_compact(float* lambda, const float4* __restrict__ pred,
                                  const uint32_t* __restrict__ keys, const uint32_t* __restrict__ uk,
                                  const uint32_t* __restrict__ off, const uint32_t* __restrict__ count,
                                  sim::DeviceParams dp, uint32_t N) {
-    lambda_ref_body(lambda, pred, idx, keys, dp, N, CompactRows{uk, off, *count});
+    lambda_ref_body(lambda, pred, idx, keys, dp, N, CompactRows{uk, off, min(*count, N)});
 }
 
 template <class Rows>
@@ -100,7 +100,7 @@ __global__ void k_delta_compact(float4* delta, const float4* __restrict__ pred, 
                                 const uint32_t* __restrict__ idx, const uint32_t* __restrict__ keys,
                                 const uint32_t* __restrict__ uk, const uint32_t* __restrict__ off,
                                 const uint32_t* __restrict__ count, sim::DeviceParams dp, uint32_t N) {
-    delta_ref_body(delta, pred, lambda, idx, keys, dp, N, CompactRows{uk, off, *count});
+    delta_ref_body(delta, pred, lambda, idx, keys, dp, N, CompactRows{uk, off, min(*count, N)});
 }
 
 // sim/pbf_delta_apply.cu:223-235 (KApplyDelta).
@@ -141,7 +141,7 @@ __global__ void k_xsph_compact(float4* vel_out, const float4* __restrict__ vel_i
                                const uint32_t* __restrict__ idx, const uint32_t* __restrict__ keys,
                                const uint32_t* __restrict__ uk, const uint32_t* __restrict__ off,
                                const uint32_t* __restrict__ count, sim::DeviceParams dp, uint32_t N) {
-    xsph_ref_body(vel_out, vel_in, pred, idx, keys, dp, N, CompactRows{uk, off, *count});
+    xsph_ref_body(vel_out, vel_in, pred, idx, keys, dp, N, CompactRows{uk, off, min(*count, N)});
 }
 
 }  // namespace

@@ -573,7 +573,9 @@ uint32_t Simulator::takeDeviceError() {
     uint32_t e = 0;
     cudaStreamSynchronize(m_stream);
     cudaMemcpy(&e, m_bufs.d_err, sizeof(e), cudaMemcpyDeviceToHost);
-    if (e) cudaMemset(m_bufs.d_err, 0, sizeof(uint32_t));
+    // cleared on the simulator's stream, so the clear is ordered before the
+    // next step's launches (which run on that stream, not the legacy one)
+    if (e) cudaMemsetAsync(m_bufs.d_err, 0, sizeof(uint32_t), m_stream);
     return e;
 }
 

@@ -209,6 +209,8 @@ _ORACLE_SIGS = {
     "oracle_step_f64": ([C.POINTER(SimParams), _I, _VP, _VP, _U32], _I),
     "oracle_density_stats_f32pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
     "oracle_density_stats_f64pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
+    "oracle_dam_break_params": ([_F, _F, _F, _I, _U32, C.POINTER(SimParams)], _I),
+    "oracle_seed_lattice": ([_VP, _U32, _U32, _U32, _F, _F, _F, _F, _F, C.c_uint64, C.POINTER(GridBounds)], None),
 }
 
 
@@ -282,6 +284,22 @@ def dam_break_params(box, iters: int = 2, num_particles: int = 0) -> SimParams:
     p = SimParams()
     check(load().pbf_dam_break_params(box[0], box[1], box[2], iters, num_particles, C.byref(p)), "dam_break_params")
     return p
+
+
+def oracle_dam_break_params(orc, box, iters: int = 2, num_particles: int = 0) -> SimParams:
+    """dam_break_params from the oracle's restatement (no product library)."""
+    p = SimParams()
+    if orc.oracle_dam_break_params(box[0], box[1], box[2], iters, num_particles, C.byref(p)) != 0:
+        raise ValueError("invalid dam-break box or iteration count")
+    return p
+
+
+def oracle_seed_lattice(orc, nx, ny, nz, origin, spacing, jitter, seed, params: SimParams) -> np.ndarray:
+    """seed_lattice from the oracle's restatement (no product library)."""
+    out = np.zeros((nx * ny * nz, 4), dtype=np.float32)
+    orc.oracle_seed_lattice(ptr(out), nx, ny, nz, origin[0], origin[1], origin[2], spacing, jitter, seed,
+                            C.byref(params.grid))
+    return out
 
 
 def device_params(p: SimParams) -> DeviceParams:

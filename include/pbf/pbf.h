@@ -129,7 +129,11 @@ int pbf_cell_compact_scratch_query(size_t* bytes, uint32_t N);
 /* sim/cell_compact.cu:187-231 LaunchCellRangesCompact: uniqueKeys[m],
  * offsets[m] = first sorted position of segment m, offsets[M] = N,
  * *compactCount = M.  Segment starts are found with __match_any_sync and
- * placed with a single-pass decoupled look-back scan. */
+ * placed with a single-pass decoupled look-back scan.  Its waits are
+ * bounded: if one gives up (a GPU that starved a predecessor tile for over
+ * 2^22 polls), *compactCount is set to 0xFFFFFFFF and the table is invalid;
+ * this library's compact-table launchers clamp such a count to N, so they
+ * stay in bounds. */
 int pbf_launch_cell_ranges_compact(void* d_scratch, size_t scratchBytes,
                                    uint32_t* uniqueKeys, uint32_t* offsets,
                                    uint32_t* compactCount,
@@ -144,9 +148,12 @@ int pbf_launch_cell_ranges_compact(void* d_scratch, size_t scratchBytes,
  * only inputs and outputs.  At most 16,777,216 keys per call (larger N:
  * PBF_ERR_UNSUPPORTED, nothing launched).  The first call on a device looks
  * up the array's device address (once per device, with that device current);
- * make that first call before any stream capture.  All calls share the array:
- * each clears what must start at zero, but calls that overlap on the GPU
- * race - serialize them. */
+ * make that first call before any stream capture; the address is looked up
+ * again when the current device's context changes (e.g. after
+ * cudaDeviceReset).  All calls share the array: each clears what must start
+ * at zero, but calls that overlap on the GPU race - serialize them.  A
+ * look-back that gives up is reported as in pbf_launch_cell_ranges_compact
+ * (*compactCount = 0xFFFFFFFF). */
 int pbf_launch_cell_ranges_compact_noalloc(uint32_t* uniqueKeys, uint32_t* offsets,
                                            uint32_t* compactCount,
                                            const uint32_t* keysSorted, uint32_t N,

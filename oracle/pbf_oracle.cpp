@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <random>
 #include <vector>
 
 #ifdef _OPENMP
@@ -756,6 +757,98 @@ void oracle_density_stats_f32pos(const pbf_sim_params* p, const float4* pos, uin
 
 void oracle_density_stats_f64pos(const pbf_sim_params* p, const double* pos4, uint32_t N, double out[4]) {
     density_stats_impl(*p, pos4, N, out);
+}
+
+int oracle_dam_break_params(float bx, float by, float bz, int solver_iters, uint32_t num_particles,
+                            pbf_sim_params* out) {
+    if (!out || !(bx > 0.f) || !(by > 0.f) || !(bz > 0.f) || solver_iters < 0) return 1;
+    pbf_sim_params sp;
+    std::memset(&sp, 0, sizeof(sp));
+    const float r = 0.005f, spacing = 0.01f, h = 2.5f * r;
+    sp.numParticles = sp.maxParticles = num_particles;
+    sp.gravity.x = 0.f;
+    sp.gravity.y = -9.8f;
+    sp.gravity.z = 0.f;
+    sp.dt = 1.0f / 120.0f;
+    sp.cfl = 0.45f;
+    sp.solverIters = solver_iters;
+    sp.maxNeighbors = 64;
+    sp.sortEveryN = 1;
+    sp.boundaryRestitution = 0.f;
+    sp.particleMass = 1000.0f * spacing * spacing * spacing;
+    // tuning: sim/parameters.h:28-56 defaults, then the dam-break values
+    pbf_tuning& t = sp.pbf;
+    t.scorr_enable = 1;
+    t.scorr_k = 0.1f;
+    t.scorr_n = 4.0f;
+    t.scorr_dq_h = 0.2f;
+    t.wq_min = 1e-12f;
+    t.scorr_min = -0.25f;
+    t.grad_r_eps = 1e-6f;
+    t.lambda_denom_eps = 100.0f;
+    t.compliance = 0.f;
+    t.xpbd_enable = 0;
+    t.enable_lambda_clamp = 1;
+    t.lambda_max_abs = 50.0f;
+    t.enable_disp_clamp = 1;
+    t.disp_clamp_max_h = 0.05f;
+    t.enable_relax = 1;
+    t.relax_omega = 0.75f;
+    t.xsph_gate_enable = 0;
+    t.xsph_n_min = 0;
+    t.xsph_n_max = 8;
+    t.lambda_warm_start_enable = 0;
+    t.lambda_warm_start_decay = 0.5f;
+    t.semi_implicit_integration_enable = 0;
+    sp.xsph_c = 0.01f;
+    // kernel coefficients, sim/parameters.h:94-107 (FP32, same operation order)
+    pbf_kernel_coeffs& kc = sp.kernel;
+    const float pi = 3.14159265358979323846f;
+    kc.h = h;
+    kc.inv_h = 1.0f / h;
+    kc.h2 = h * h;
+    const float h3 = h * kc.h2, h6 = h3 * h3, h9 = h6 * h3;
+    kc.poly6 = 315.0f / (64.0f * pi * h9);
+    kc.spiky = 15.0f / (pi * h6);
+    kc.visc = 15.0f / (2.0f * pi * h3);
+    float density = 0.f;
+    for (int n = 0; n < 6; ++n) {
+        const float r2 = spacing * spacing;
+        const float hr2 = kc.h2 - r2;
+        density += sp.particleMass * kc.poly6 * hr2 * hr2 * hr2;
+    }
+    sp.restDensity = density;
+    sp.grid.mins.x = sp.grid.mins.y = sp.grid.mins.z = 0.f;
+    sp.grid.maxs.x = bx;
+    sp.grid.maxs.y = by;
+    sp.grid.maxs.z = bz;
+    sp.grid.cellSize = std::fmax(1e-6f, 1.0f * h);
+    compute_dims(sp.grid);
+    sp.grid.dim.x = std::max(sp.grid.dim.x, 1);
+    sp.grid.dim.y = std::max(sp.grid.dim.y, 1);
+    sp.grid.dim.z = std::max(sp.grid.dim.z, 1);
+    *out = sp;
+    return 0;
+}
+
+void oracle_seed_lattice(float4* out, uint32_t nx, uint32_t ny, uint32_t nz, float ox, float oy, float oz,
+                         float spacing, float jitter, uint64_t seed, const pbf_grid_bounds* box) {
+    std::mt19937_64 rng(seed);
+    auto unit = [&]() { return double(rng() >> 11) * (1.0 / 9007199254740992.0); };
+    const pbf_grid_bounds& g = *box;
+    size_t id = 0;
+    for (uint32_t iz = 0; iz < nz; ++iz)
+        for (uint32_t iy = 0; iy < ny; ++iy)
+            for (uint32_t ix = 0; ix < nx; ++ix) {
+                const float jx = float((2.0 * unit() - 1.0) * double(jitter));
+                const float jy = float((2.0 * unit() - 1.0) * double(jitter));
+                const float jz = float((2.0 * unit() - 1.0) * double(jitter));
+                out[id].x = std::fmin(std::fmax(ox + float(ix) * spacing + jx, g.mins.x), g.maxs.x);
+                out[id].y = std::fmin(std::fmax(oy + float(iy) * spacing + jy, g.mins.y), g.maxs.y);
+                out[id].z = std::fmin(std::fmax(oz + float(iz) * spacing + jz, g.mins.z), g.maxs.z);
+                out[id].w = 1.0f;
+                ++id;
+            }
 }
 
 }  // extern "C"

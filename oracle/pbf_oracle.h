@@ -104,6 +104,23 @@ void oracle_density_stats_f32pos(const pbf_sim_params* p, const float4* pos,
 void oracle_density_stats_f64pos(const pbf_sim_params* p, const double* pos4,
                                  uint32_t N, double out[4]);
 
+/* Scene generation for the CPU arm, so that it needs no product library.
+ * The dam-break parameters: particle radius 0.005 m, spacing 2r, h = 2.5 r
+ * (engine/core/console.cpp:198-267), mass 1000 spacing^3, dt 1/120,
+ * gravity -9.8 y, maxNeighbors 64, restitution 0, s_corr k 0.1 n 4
+ * dq 0.2 h, lambda eps 100, XSPH 0.01, the other tuning fields at their
+ * sim/parameters.h defaults, rho0 = the lambda-kernel density of an interior
+ * particle of the unjittered lattice (its 6 face neighbours), grid [0,b] with
+ * cell size h.  Returns 0, or 1 for an invalid box / iteration count. */
+int oracle_dam_break_params(float bx, float by, float bz, int solver_iters,
+                            uint32_t num_particles, pbf_sim_params* out);
+/* nx*ny*nz particles at origin + index*spacing (x fastest), each axis
+ * jittered by (2u - 1)*jitter with u = (mt19937_64 output >> 11) / 2^53,
+ * three draws per particle in x, y, z order, clamped to the box, w = 1. */
+void oracle_seed_lattice(float4* out, uint32_t nx, uint32_t ny, uint32_t nz, float ox,
+                         float oy, float oz, float spacing, float jitter, uint64_t seed,
+                         const pbf_grid_bounds* box);
+
 #ifdef __cplusplus
 }
 #endif

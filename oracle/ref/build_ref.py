@@ -6,7 +6,9 @@ under oracle/_ref/, which is git-ignored.  Device code only: the host side is
 oracle/ref/ref_harness.cu, which loads these images with the CUDA driver API
 and launches the kernels in the reference phase order.
 
-Run here (where the reference sources exist):  python oracle/ref/build_ref.py
+Run where the reference sources exist:  python oracle/ref/build_ref.py
+[REFERENCE_ROOT].  The reference checkout is the argument, else the
+PBF_REFERENCE_ROOT environment variable, else /root/reference.
 """
 import os
 import subprocess
@@ -15,7 +17,17 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-SRC = "/root/reference/sim"
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root(argv=None) -> str:
+    """The reference checkout: argument, then $PBF_REFERENCE_ROOT, then the default."""
+    if argv:
+        return argv[0]
+    return os.environ.get("PBF_REFERENCE_ROOT", DEFAULT_REFERENCE_ROOT)
+
+
+SRC = os.path.join(reference_root(sys.argv[1:] if __name__ == "__main__" else None), "sim")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 # The kernels of the step (sim/phases.cpp, sim/post_ops.cpp).  The build
 # mirrors the reference's: no fast-math, default FMA contraction.

@@ -55,3 +55,43 @@ def test_reference_arm_other_ranks_print_nothing():
 def test_warmup_floor():
     with pytest.raises(SystemExit):
         bench.main(["--warmup", "2"])
+
+
+def test_reference_arm_config_is_ours():
+    """Both arms describe the workload with the same config object."""
+    rc, lines = run_main(["--impl", "reference", "--config", "c1", "--steps", "2", "--warmup", "3"])
+    d = json.loads(lines[0])
+    args = bench.argparse.Namespace(steps=2, warmup=3)
+    import pbfx
+
+    orc = pbfx.load_oracle()
+    p, pos, _ = bench.scene(None, bench.CONFIGS["c1"], orc=orc)
+    assert d["config"] == bench.config_record(bench.CONFIGS["c1"], pos.shape[0], pbfx.num_cells(p), 1, args)
+
+
+def test_reference_arm_loads_no_product_library(built):
+    """The CPU arm runs the oracle alone: the product library is never mapped."""
+    import subprocess
+
+    code = ("import sys, io, contextlib; sys.path.insert(0, %r); import bench\n"
+            "with contextlib.redirect_stdout(io.StringIO()):\n"
+            "    bench.main(['--impl', 'reference', '--config', 'c1', '--steps', '1', '--warmup', '3'])\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('product' if 'libpbf_gb300' in maps else 'clean', 'oracle' if 'liboracle' in maps else '')\n"
+            % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == ["clean", "oracle"], r.stdout
+
+
+@pytest.mark.parametrize("config", ["c1", "c2"])
+def test_oracle_scene_generation_matches_library(lib, orc, config):
+    """The oracle's restated scene generation gives the library's bits."""
+    import ctypes as C
+
+    cfg = bench.CONFIGS[config]
+    p_lib, pos_lib, _ = bench.scene(lib, cfg)
+    p_orc, pos_orc, _ = bench.scene(None, cfg, orc=orc)
+    assert bytes(p_lib) == bytes(p_orc)
+    assert C.sizeof(p_lib) == C.sizeof(p_orc)
+    assert pos_lib.tobytes() == pos_orc.tobytes()

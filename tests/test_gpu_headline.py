@@ -1,0 +1,128 @@
+"""The timed workloads themselves, pinned to the reference and to the oracle.
+
+* C2, the workload bench.py times (1,048,576 particles: a 128x64x128 jittered
+  lattice in the [0,2]x[0,1]x[0,2] box, 2 solver iterations), hashed and
+  dense grids: the fused step (pbf_create / pbf_step) and the reference's own
+  kernels (sim/hash_keys.cu, sim/cell_compact.cu, sim/cell_ranges.cu,
+  sim/pbf_lambda.cu, sim/pbf_delta_apply.cu, sim/xsph.cu, built from its
+  sources and driven in its phase order by oracle/ref/ref_harness.cu) run the
+  same 20 steps from the seeded lattice.  Sorted keys, permutation, the last
+  iteration's lambda, positions and velocities are bit-identical after steps
+  1, 10 and 20.
+* C3 (9,437,184 particles, 4 iterations): five consecutive steps from the
+  state after 20 steps, each checked against the FP32 oracle stepped from the
+  GPU's own state (keys, permutation and cell tables bit-exact; state within
+  the bars of tests/parity.py).
+* C4: three ensemble scenes with tilted gravity and 3 iterations stepped as
+  one batch, each scene checked per step against the oracle.
+"""
+import numpy as np
+import pytest
+
+import pbfx
+from parity import STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close, step_lambda_tol
+
+pytestmark = pytest.mark.gpu
+
+
+def c2_scene(lib):
+    n = 128 * 64 * 128
+    p = pbfx.dam_break_params((2.0, 1.0, 2.0), 2, n)
+    pos = pbfx.seed_lattice(lib, 128, 64, 128, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
+    return p, pos
+
+
+@pytest.mark.parametrize("hashed", [True, False], ids=["hashed", "dense"])
+def test_c2_fused_step_is_bit_identical_to_reference_kernels(gpu, lib, hashed):
+    ref = pbfx.load_ref()
+    if ref is None:
+        pytest.skip("reference device images not present in this checkout")
+    p, pos = c2_scene(lib)
+    rp, rv = pos.copy(), np.zeros_like(pos)
+    checked = []
+    with pbfx.Sim(lib, p, hashed=hashed) as s:
+        s.upload(pos, np.zeros_like(pos))
+        for k in range(1, 21):
+            trace = k in (1, 10, 20)
+            rtr = pbfx.ref_step(ref, p, hashed, rp, rv, trace=trace)
+            s.step()
+            if not trace:
+                continue
+            np.testing.assert_array_equal(s.fetch(pbfx.DBG_KEYS_SORTED), rtr["keys_sorted"])
+            np.testing.assert_array_equal(s.fetch(pbfx.DBG_PERM), rtr["perm"])
+            if hashed:
+                m = int(s.fetch(pbfx.DBG_COMPACT_COUNT)[0])
+                np.testing.assert_array_equal(s.fetch(pbfx.DBG_UNIQUE_KEYS)[:m], rtr["unique_keys"])
+                np.testing.assert_array_equal(s.fetch(pbfx.DBG_OFFSETS)[: m + 1], rtr["offsets"])
+            else:
+                np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_START), rtr["cell_start"])
+                np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_END), rtr["cell_end"])
+            np.testing.assert_array_equal(s.fetch(pbfx.DBG_LAMBDA), rtr["lambda"])
+            gp, gv = s.download()
+            np.testing.assert_array_equal(gp, rp)
+            np.testing.assert_array_equal(gv, rv)
+            checked.append(k)
+    assert checked == [1, 10, 20]
+
+
+def oracle_compare_step(s, orc, p, hashed):
+    """One GPU step checked against the oracle stepped from the GPU's state."""
+    cur_pos, cur_vel = s.download()
+    opos, ovel = cur_pos.copy(), cur_vel.copy()
+    tr = pbfx.oracle_step(orc, p, hashed, opos, ovel)
+    s.step()
+    np.testing.assert_array_equal(s.fetch(pbfx.DBG_KEYS_SORTED), tr["keys_sorted"])
+    np.testing.assert_array_equal(s.fetch(pbfx.DBG_PERM), tr["perm"])
+    if hashed:
+        m = int(s.fetch(pbfx.DBG_COMPACT_COUNT)[0])
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_UNIQUE_KEYS)[:m], tr["unique_keys"])
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_OFFSETS)[: m + 1], tr["offsets"])
+    else:
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_START), tr["cell_start"])
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_END), tr["cell_end"])
+    gpos, gvel = s.download()
+    pbfx.assert_close(s.fetch(pbfx.DBG_LAMBDA), tr["lambda"], step_lambda_tol(p.solverIters), "lambda",
+                      floor_frac=STEP_LAMBDA_FLOOR)
+    pbfx.assert_close(gpos, opos, STEP_POS, "positions")
+    assert_velocities_close(gvel, ovel, opos, p.dt)
+
+
+def test_c3_slice_against_oracle(gpu, lib, orc):
+    """C3: an 8,388,608-particle slab (256x128x256 lattice) and a 1,048,576-
+    particle block (128x64x128) 0.5 m above it at a seeded (x, z), in the
+    [0,3]x[0,2.5]x[0,3] box, 4 iterations, hashed grid, list capacity 1024
+    (bench.py --config c3): steps 21..25 against the oracle."""
+    import bench
+
+    cfg = bench.CONFIGS["c3"]
+    p, pos, vel = bench.scene(lib, cfg)
+    assert pos.shape[0] == 9_437_184 and p.solverIters == 4
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        s.set_list_capacity(cfg["list_capacity"])
+        s.upload(pos, vel)
+        s.step(20)
+        for _ in range(5):
+            oracle_compare_step(s, orc, p, hashed=True)
+
+
+def test_c4_scenes_against_oracle(gpu, lib, orc):
+    """Three seeded C4 scenes (log-uniform sizes, boxes U[0.3,1]^3, gravity
+    tilted up to 15 degrees, 3 iterations) stepped as one ensemble: every scene
+    checked per step against the oracle stepped from the ensemble's state."""
+    scenes, pos = pbfx.ensemble_scenes(lib, 3, seed=0xC4C4, iters_choices=(3,))
+    assert all(abs(sc.gravity.x) + abs(sc.gravity.z) > 0 for sc in scenes)
+    with pbfx.Ensemble(lib, scenes) as e:
+        e.upload(pos, np.zeros_like(pos))
+        off = e.offsets.astype(np.int64)
+        for k in range(12):
+            cur_pos, cur_vel = e.download()
+            e.step()
+            gpos, gvel = e.download()
+            if k % 3:
+                continue
+            for si, sc in enumerate(scenes):
+                a, b = off[si], off[si + 1]
+                opos, ovel = cur_pos[a:b].copy(), cur_vel[a:b].copy()
+                pbfx.oracle_step(orc, sc, True, opos, ovel, trace=False)
+                pbfx.assert_close(gpos[a:b], opos, STEP_POS, "scene %d positions" % si)
+                assert_velocities_close(gvel[a:b], ovel, opos, sc.dt)
