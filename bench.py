@@ -261,7 +261,8 @@ def config_record(cfg, n: int, nc: int, world: int, args) -> dict:
             "grid": "hashed" if cfg["hashed"] else "dense", "parallelism": "replicas" if world > 1 else "single",
             "timed_steps": "steps %d..%d of the run from the seeded lattice" % (args.warmup,
                                                                               args.warmup + args.steps - 1),
-            "l2": "flushed before every timed step (256 MiB write, untimed)"}
+            "l2": "flushed before every timed step (256 MiB write, untimed)",
+            "arithmetic": getattr(args, "math", "exact")}
 
 
 def cpu_rate(orc, p, hashed, pos, vel, budget_s: float, max_steps: int):
@@ -498,6 +499,8 @@ def run_ours(args, cfg, world, rank, local):
     sim = pbfx.Sim(lib, p, hashed=hashed)
     if "list_capacity" in cfg:
         sim.set_list_capacity(cfg["list_capacity"])
+    if args.math == "fast":
+        sim.set_math_mode(pbfx.PBF_MATH_FAST)
     sim.upload(pos, vel)
     stream = torch.cuda.ExternalStream(sim.stream_ptr())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -582,6 +585,26 @@ def run_ours(args, cfg, world, rank, local):
     e2e_s = time.perf_counter() - t0
     e2e_total, e2e_units = aggregate(e2e_s, float(n) * e2e_steps, world)
     e2e_pos, _ = sim.download()
+    # The other arithmetic mode over the same window (same state, same L2
+    # flushes), for comparison.
+    other = "fast" if args.math == "exact" else "exact"
+    sim.set_math_mode(pbfx.PBF_MATH_FAST if other == "fast" else pbfx.PBF_MATH_EXACT)
+    sim.upload(snap_pos, snap_vel)
+    pbfx.check(lib.pbf_step(sim.h, pp))  # graph capture of the other mode, then back to the window's start
+    sim.upload(snap_pos, snap_vel)
+    torch.cuda.synchronize()
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev2[k][0].record(stream)
+            lib.pbf_step(sim.h, pp)
+            ev2[k][1].record(stream)
+    pbfx.check(lib.pbf_synchronize(sim.h))
+    torch.cuda.synchronize()
+    other_ms = sum(a.elapsed_time(b) for a, b in ev2) / args.steps
+    other_pos, _ = sim.download()
+    sim.set_math_mode(pbfx.PBF_MATH_FAST if args.math == "fast" else pbfx.PBF_MATH_EXACT)
     launches = sim.launches_per_step() * args.steps
     list_cap, list_longest, list_overflowed = sim.list_stats()
     sim.close()
@@ -626,6 +649,14 @@ def run_ours(args, cfg, world, rank, local):
         "phase_sum_ms": round(total_phase, 5),
         "profiled_window_identical_to_timed_run": bool(np.array_equal(prof_pos, final_pos)),
         "density_error": dens,
+        "other_arithmetic": {
+            "arithmetic": other, "value": n / (other_ms * 1e-3), "unit": UNIT, "ms_per_step": other_ms,
+            "speedup_vs_line": (1e3 * total_s / args.steps) / other_ms,
+            "final_positions_max_abs_diff_vs_line": float(np.max(np.abs(other_pos[:, :3].astype(np.float64) -
+                                                                        final_pos[:, :3]))),
+            "what": "the same window timed in the other arithmetic mode (pbf_set_math_mode); exact = bit-identical "
+                    "to the reference kernels, fast = within 1e-5 relative per step (tests/test_gpu_fast_math.py); "
+                    "over 20+ steps the two trajectories separate as the dynamics amplify rounding"},
         "step_ms": {"first": round(step_ms[0], 4), "median": round(statistics.median(step_ms), 4),
                     "max": round(max(step_ms), 4), "last": round(step_ms[-1], 4)},
         "gpu_launches": launches,
@@ -946,6 +977,9 @@ def main(argv=None):
     ap.add_argument("--autotune-steps", type=int, default=3,
                     help="steps per tile shape for the autotuner after warm-up (0: keep the default shape)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--math", choices=["exact", "fast"], default="exact",
+                    help="arithmetic of the lambda / delta passes: exact (bit-identical to the reference kernels) "
+                         "or fast (within 1e-5 relative per step)")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=0,

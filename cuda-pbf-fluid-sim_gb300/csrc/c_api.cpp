@@ -429,6 +429,17 @@ int pbf_profile_step(pbf_sim* h, const pbf_sim_params* p, float* ms, const char*
 
 int pbf_launches_per_step(pbf_sim* h) { return h ? h->sim.launchesPerStep() : 0; }
 
+int pbf_set_math_mode(pbf_sim* h, int mode) {
+    if (!h || (mode != PBF_MATH_EXACT && mode != PBF_MATH_FAST)) return PBF_ERR_INVALID;
+    return h->sim.setMathMode(mode) ? PBF_OK : PBF_ERR_INVALID;
+}
+
+int pbf_get_math_mode(pbf_sim* h, int* mode) {
+    if (!h || !mode) return PBF_ERR_INVALID;
+    *mode = h->sim.mathMode();
+    return PBF_OK;
+}
+
 int pbf_set_neighbour_list_capacity(pbf_sim* h, uint32_t entries) {
     if (!h) return PBF_ERR_INVALID;
     if (entries > (1u << 20)) return PBF_ERR_INVALID;

@@ -100,6 +100,7 @@ struct pbf_ensemble {
              *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr;
     uint32_t nbrCap = 0;
     int tile = 0;  // tile shape of the list passes
+    bool fast = false;  // arithmetic of the lambda / delta passes (PBF_MATH_FAST)
     pbf::SceneInfo* scenes = nullptr;
     void* sortTemp = nullptr;
     size_t sortBytes = 0;
@@ -141,6 +142,7 @@ struct pbf_ensemble {
         m.nbr_cap = nbrCap;
         m.err = err;
         m.tile = tile;
+        m.fast = fast;
         return m;
     }
 
@@ -191,6 +193,18 @@ struct pbf_ensemble {
         exec = nullptr;
         graph = nullptr;
         tile = id;
+        return capture();
+    }
+
+    // Replaces the step graph with one for arithmetic mode `f`.
+    int set_fast(bool f) {
+        if (f == fast && exec) return PBF_OK;
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return PBF_ERR_CUDA;
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        fast = f;
         return capture();
     }
 };
@@ -360,6 +374,17 @@ int pbf_ensemble_synchronize(pbf_ensemble* e) {
 int pbf_ensemble_set_tile_shape(pbf_ensemble* e, int id) {
     if (!e || id < 0 || id >= pbf::fused_tile_shape_count()) return PBF_ERR_INVALID;
     return e->set_tile(id);
+}
+
+int pbf_ensemble_set_math_mode(pbf_ensemble* e, int mode) {
+    if (!e || (mode != PBF_MATH_EXACT && mode != PBF_MATH_FAST)) return PBF_ERR_INVALID;
+    return e->set_fast(mode == PBF_MATH_FAST);
+}
+
+int pbf_ensemble_get_math_mode(pbf_ensemble* e, int* mode) {
+    if (!e || !mode) return PBF_ERR_INVALID;
+    *mode = e->fast ? PBF_MATH_FAST : PBF_MATH_EXACT;
+    return PBF_OK;
 }
 
 int pbf_ensemble_get_tile_shape(pbf_ensemble* e, int* id) {

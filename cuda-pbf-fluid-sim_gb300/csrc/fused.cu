@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 #include "grid.cuh"
 #include "pbf_common.cuh"
@@ -651,7 +652,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
 }
 
 // lambda of iteration `it` for every slot whose scene runs that iteration.
-template <class Scenes, class Sh>
+template <class Scenes, class Sh, bool kFast>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf,
@@ -676,21 +677,21 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
+            a = lambda_queued_acc<kQueue, Sh::kTile, kFast>(active, sc, pi,
                                              ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                              StagedData{sp, nullptr}, q16);
         else
-            a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
+            a = lambda_queued_acc<kQueue, Sh::kTile, kFast>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
     } else if (staged) {
         int cx, cy, cz;
         decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            a = lambda_of_acc(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
+            a = lambda_of_acc<kFast>(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
                 j = k;
                 return __ldg(pred + k);
             });
     } else {
-        a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
+        a = lambda_queued_acc<kQueue, Sh::kTile, kFast>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
     }
     if (!active) return;
     // the neighbour sums, for the adjoint's replay
@@ -705,7 +706,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
 // post-solve boundary (e = 0) and computes v = (x - p)/dt; a scene past its
 // iterations carries its prediction through, and a scene without iterations
 // gets boundary and velocity in pass 0.
-template <class Scenes, class Sh>
+template <class Scenes, class Sh, bool kFast>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, const float4* __restrict__ pred,
                                                  const float* __restrict__ lam, const uint32_t* __restrict__ key_s,
                                                  const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
@@ -734,24 +735,24 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
     if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            d = delta_queued_sum<kQueue, Sh::kTile>(active, sc, pi, lam_i,
+            d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i,
                                             ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                             w_q, StagedData{sp, nullptr}, q16);
         else
-            d = delta_queued_sum<kQueue, Sh::kTile>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
+            d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
                                             q32);
     } else if (staged) {
         int cx, cy, cz;
         decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            d = delta_of_sum(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb + v.cellOffset},
+            d = delta_of_sum<kFast>(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb + v.cellOffset},
                          [&](uint32_t k, uint32_t& j, float& lj) {
                              j = k;
                              lj = __ldg(lam + k);
                              return __ldg(pred + k);
                          });
     } else {
-        d = delta_queued_sum<kQueue, Sh::kTile>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
+        d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
     }
     // the neighbour sum, for the adjoint's replay (which needs the displacement
     // before the clamp)
@@ -1042,15 +1043,31 @@ cudaError_t with_tile_shape(int id, F&& f) {
     }
 }
 
-template <class Sh>
-cudaError_t prepare_shape() {
-    const int solve = int(Sh::kSolveSmem), commit = int(Sh::kCommitSmem);
+// Calls f with std::integral_constant<bool, fast> for the arithmetic mode.
+template <class F>
+cudaError_t with_math(bool fast, F&& f) {
+    return fast ? f(std::true_type{}) : f(std::false_type{});
+}
+
+template <class Sh, bool kFast>
+cudaError_t prepare_solve() {
+    const int solve = int(Sh::kSolveSmem);
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_lambda<OneScene, Sh>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_lambda<ManyScenes, Sh>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<OneScene, Sh>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<ManyScenes, Sh>, a, solve)) != cudaSuccess ||
+    if ((e = cudaFuncSetAttribute(k_lambda<OneScene, Sh, kFast>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_lambda<ManyScenes, Sh, kFast>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<OneScene, Sh, kFast>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<ManyScenes, Sh, kFast>, a, solve)) != cudaSuccess)
+        return e;
+    return cudaSuccess;
+}
+
+template <class Sh>
+cudaError_t prepare_shape() {
+    const int commit = int(Sh::kCommitSmem);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e;
+    if ((e = prepare_solve<Sh, false>()) != cudaSuccess || (e = prepare_solve<Sh, true>()) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<OneScene, true, Sh>, a, commit)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<OneScene, false, Sh>, a, commit)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<ManyScenes, true, Sh>, a, commit)) != cudaSuccess)
@@ -1113,15 +1130,17 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
     const OneScene sc = one_scene(b, sh, it);
     return with_tile_shape(sh.tile, [&](auto shape) {
         using Sh = decltype(shape);
-        const unsigned g = blocks_for(sh.N, Sh::kTile);
-        if (which == 0)
-            k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s,
-                                                                         list_bufs(b, sh), b.err, b.lambda_acc);
-        else
-            k_delta<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt,
-                                                                        b.pos_s, b.vel_s, list_bufs(b, sh),
-                                                                        b.delta_sum);
-        return cudaGetLastError();
+        return with_math(sh.fast, [&](auto fast) {
+            constexpr bool kFast = decltype(fast)::value;
+            const unsigned g = blocks_for(sh.N, Sh::kTile);
+            if (which == 0)
+                k_lambda<OneScene, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
+                    it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh), b.err, b.lambda_acc);
+            else
+                k_delta<OneScene, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
+                    it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s, list_bufs(b, sh), b.delta_sum);
+            return cudaGetLastError();
+        });
     });
 }
 
@@ -1181,14 +1200,17 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
-        const unsigned g = blocks_for(m.N, Sh::kTile);
-        if (which == 0)
-            k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N, m.lam_s,
-                                                                           lb, m.err, nullptr);
-        else
-            k_delta<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.lam_s, m.key_s, m.lb, sc, m.N,
-                                                                          nxt, m.pos_s, m.vel_s, lb, nullptr);
-        return cudaGetLastError();
+        return with_math(m.fast, [&](auto fast) {
+            constexpr bool kFast = decltype(fast)::value;
+            const unsigned g = blocks_for(m.N, Sh::kTile);
+            if (which == 0)
+                k_lambda<ManyScenes, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N,
+                                                                                    m.lam_s, lb, m.err, nullptr);
+            else
+                k_delta<ManyScenes, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
+                    it, cur, m.lam_s, m.key_s, m.lb, sc, m.N, nxt, m.pos_s, m.vel_s, lb, nullptr);
+            return cudaGetLastError();
+        });
     });
 }
 

@@ -82,6 +82,7 @@ pbf::FusedShape fused_shape(const DeviceBuffers& b, const GridBuffers& g, const 
     s.xsph = b.xsphEnabled;
     s.list_span = pbf::list_span_for(p);
     s.tile = b.tileShape;
+    s.fast = b.mathMode == 1;
     return s;
 }
 
@@ -422,6 +423,15 @@ int Simulator::launchesPerStep() const {
     if (m_bufs.nbrListCap > 0) n += pbf::fused_list_builds(fused_shape(m_bufs, m_grid, m_params));
     n += 1; /*commit*/
     return n;
+}
+
+bool Simulator::setMathMode(int mode) {
+    if (mode != 0 && mode != 1) return false;
+    if (mode == m_bufs.mathMode) return true;
+    if (m_stream) cudaStreamSynchronize(m_stream);
+    m_bufs.mathMode = mode;
+    m_graphDirty = true;
+    return true;
 }
 
 bool Simulator::setTileShape(int id) {

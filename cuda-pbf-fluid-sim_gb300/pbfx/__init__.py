@@ -28,6 +28,8 @@ PBF_ERR_NONFINITE = 5
 PBF_ERR_UNSUPPORTED = 6
 PBF_GRID_DENSE = 0
 PBF_GRID_HASHED = 1
+PBF_MATH_EXACT = 0
+PBF_MATH_FAST = 1
 
 DBG_KEYS_SORTED = 0
 DBG_PERM = 1
@@ -190,6 +192,10 @@ _SIGS = {
     "pbf_ensemble_set_tile_shape": ([_VP, _I], _I),
     "pbf_ensemble_get_tile_shape": ([_VP, C.POINTER(_I)], _I),
     "pbf_ensemble_autotune": ([_VP, _I, C.POINTER(_F), C.POINTER(_I)], _I),
+    "pbf_set_math_mode": ([_VP, _I], _I),
+    "pbf_get_math_mode": ([_VP, C.POINTER(_I)], _I),
+    "pbf_ensemble_set_math_mode": ([_VP, _I], _I),
+    "pbf_ensemble_get_math_mode": ([_VP, C.POINTER(_I)], _I),
 }
 
 _ORACLE_SIGS = {
@@ -209,6 +215,7 @@ _ORACLE_SIGS = {
     "oracle_step_f64": ([C.POINTER(SimParams), _I, _VP, _VP, _U32], _I),
     "oracle_density_stats_f32pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
     "oracle_density_stats_f64pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
+    "oracle_step_jvp_f64": ([C.POINTER(SimParams), _I, _VP, _VP, _VP, _VP, C.c_double, _U32, _I], _I),
     "oracle_dam_break_params": ([_F, _F, _F, _I, _U32, C.POINTER(SimParams)], _I),
     "oracle_seed_lattice": ([_VP, _U32, _U32, _U32, _F, _F, _F, _F, _F, C.c_uint64, C.POINTER(GridBounds)], None),
 }
@@ -405,6 +412,14 @@ class Sim:
     def set_tile_shape(self, shape: int):
         check(self.lib.pbf_set_tile_shape(self.h, shape), "set_tile_shape")
 
+    def set_math_mode(self, mode: int):
+        check(self.lib.pbf_set_math_mode(self.h, mode), "set_math_mode")
+
+    def math_mode(self) -> int:
+        v = _I()
+        check(self.lib.pbf_get_math_mode(self.h, C.byref(v)), "get_math_mode")
+        return int(v.value)
+
     def tile_shape(self) -> int:
         v = _I()
         check(self.lib.pbf_get_tile_shape(self.h, C.byref(v)), "get_tile_shape")
@@ -490,6 +505,9 @@ class Ensemble:
 
     def set_tile_shape(self, shape: int):
         check(self.lib.pbf_ensemble_set_tile_shape(self.h, shape), "ensemble set_tile_shape")
+
+    def set_math_mode(self, mode: int):
+        check(self.lib.pbf_ensemble_set_math_mode(self.h, mode), "ensemble set_math_mode")
 
     def tile_shape(self) -> int:
         v = _I()

@@ -46,6 +46,9 @@ struct DeviceBuffers {
     // Tile shape of the list passes (particles per CTA and staged slots; the
     // results do not depend on it).
     int tileShape = 0;
+    // Arithmetic of the lambda and delta passes: 0 exact (bit-identical to
+    // the reference kernels), 1 fast (within the 1e-5 bars; PBF_MATH_FAST).
+    int mathMode = 0;
 
     bool allocate(uint32_t cap);
     // (Re)allocates the lists for `capacity` particles; entries is rounded up

@@ -134,6 +134,22 @@ inline float4 f4(float x, float y, float z, float w) {
 inline float fma_r(float a, float b, float c) { return std::fmaf(a, b, c); }
 inline double fma_r(double a, double b, double c) { return std::fma(a, b, c); }
 
+// The real-type operations of the kernels below, overloaded per type (float,
+// double, and the dual numbers of the forward-mode derivative further down).
+// max_r is std::max's (a < b) ? b : a.
+inline float floor_r(float a) { return std::floor(a); }
+inline double floor_r(double a) { return std::floor(a); }
+inline float sqrt_r(float a) { return std::sqrt(a); }
+inline double sqrt_r(double a) { return std::sqrt(a); }
+template <typename R>
+inline R max_r(R a, R b) { return (a < b) ? b : a; }
+inline bool isfinite_r(float a) { return std::isfinite(a); }
+inline bool isfinite_r(double a) { return std::isfinite(a); }
+inline float fabs_r(float a) { return std::fabs(a); }
+inline double fabs_r(double a) { return std::fabs(a); }
+inline float copysign_r(float a, float b) { return std::copysign(a, b); }
+inline double copysign_r(double a, double b) { return std::copysign(a, b); }
+
 // sim/integrate.cu:40-51 (KIntegratePred).  The GPU computes both
 // multiply-adds as single fused operations; fmaf reproduces them exactly.
 template <typename R>
@@ -201,9 +217,9 @@ void hash_keys_t(uint32_t* keys, uint32_t* idx, const V4<R>* pred, V3<R> mins, R
         R rx = (pred[i].x - mins.x) / cs;
         R ry = (pred[i].y - mins.y) / cs;
         R rz = (pred[i].z - mins.z) / cs;
-        int cx = clampi(to_int_sat(std::floor(rx)), 0, dx - 1);
-        int cy = clampi(to_int_sat(std::floor(ry)), 0, dy - 1);
-        int cz = clampi(to_int_sat(std::floor(rz)), 0, dz - 1);
+        int cx = clampi(to_int_sat(floor_r(rx)), 0, dx - 1);
+        int cy = clampi(to_int_sat(floor_r(ry)), 0, dy - 1);
+        int cz = clampi(to_int_sat(floor_r(rz)), 0, dz - 1);
         keys[i] = (uint32_t)((cz * dy + cy) * dx + cx);
         if (idx) idx[i] = (uint32_t)i;
     }
@@ -307,8 +323,8 @@ void lambda_t(R* lambda, const V4<R>* pred, const uint32_t* idx, const uint32_t*
             ++contrib;
             R hr2 = p.h2 - r2;
             density = fma_r(p.mass * p.poly6 * hr2 * hr2, hr2, density);
-            R r = std::sqrt(r2);
-            R r_safe = std::max(r, p.grad_r_eps);
+            R r = sqrt_r(r2);
+            R r_safe = max_r(r, p.grad_r_eps);
             R t = p.h - r;
             R coeff = (R(-3) * p.spiky * (t * t) / r_safe);
             R ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
@@ -320,16 +336,16 @@ void lambda_t(R* lambda, const V4<R>* pred, const uint32_t* idx, const uint32_t*
         R scale = (p.rest > R(0)) ? (p.mass / p.rest) : R(0);
         R denom = fma_r(scale * scale, sumGrad2 + gradSum2, p.lambda_denom_eps);
         if (p.compliance > R(0) && p.dt > R(0)) denom += p.compliance / (p.dt * p.dt);
-        denom = std::max(denom, p.lambda_denom_eps);
+        denom = max_r(denom, p.lambda_denom_eps);
         R lam;
         if (contrib < 2 || (sumGrad2 + gradSum2) < R(1e-12f)) {
             lam = R(0);
         } else {
             R C = (p.rest > R(0)) ? (density / p.rest - R(1)) : R(0);
             lam = -C / denom;
-            if (!std::isfinite(lam)) lam = R(0);
+            if (!isfinite_r(lam)) lam = R(0);
             if (p.enable_lambda_clamp) {
-                if (std::fabs(lam) > p.lambda_max_abs) lam = std::copysign(p.lambda_max_abs, lam);
+                if (fabs_r(lam) > p.lambda_max_abs) lam = copysign_r(p.lambda_max_abs, lam);
             }
         }
         lambda[i] = lam;
@@ -361,9 +377,9 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
             R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
             R r2 = fma_r(rz, rz, fma_r(rx, rx, ry * ry));
             if (r2 > p.h2) return true;
-            R r = std::sqrt(r2);
+            R r = sqrt_r(r2);
             R t = p.h - r;
-            R r_safe = std::max(r, p.grad_r_eps);
+            R r_safe = max_r(r, p.grad_r_eps);
             R coeff = (R(-3) * p.spiky * (t * t) / r_safe);
             R ax = coeff * rx, ay = coeff * ry, az = coeff * rz;
             R scorr = 0;
@@ -372,7 +388,7 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
                 R w = p.poly6 * hr2 * hr2 * hr2;
                 R ratio = (w_q > R(0)) ? (w / w_q) : R(0);
                 scorr = -p.scorr_k * pow_r(ratio, p.scorr_n);
-                if (p.scorr_min < R(0)) scorr = std::max(scorr, p.scorr_min);
+                if (p.scorr_min < R(0)) scorr = max_r(scorr, p.scorr_min);
             }
             R lij = (lambda[i] + lambda[j] + scorr);
             dx_ = fma_r(lij, ax, dx_);
@@ -388,7 +404,7 @@ void delta_apply_t(V4<R>* pred, V4<R>* delta, const R* lambda, const uint32_t* i
             R maxDisp2 = maxDisp * maxDisp;
             R len2 = fma_r(ez, ez, fma_r(ex, ex, ey * ey));
             if (len2 > maxDisp2) {
-                R len = std::sqrt(len2);
+                R len = sqrt_r(len2);
                 R sc = maxDisp / (len + R(1e-20f));
                 ex *= sc; ey *= sc; ez *= sc;
             }
@@ -663,6 +679,78 @@ void density_stats_impl(const pbf_sim_params& sp0, const double* xyz4, uint32_t 
     out[3] = sumNb / n;
 }
 
+// ----------------------------------------------- forward-mode derivative
+// Dual numbers v + d e (e^2 = 0) in FP64: running the step on them carries the
+// exact directional derivative of the FP64 step beside its value, with every
+// branch (neighbour sets, clamps, caps, boundary) decided by the values, as
+// the step itself decides it.  This is the FP64 reference the adjoint's
+// vector-Jacobian products are checked against.
+struct Dual {
+    double v, d;
+    Dual() = default;
+    Dual(double x) : v(x), d(0.0) {}  // NOLINT: constants and FP32 parameters
+    Dual(double x, double dx) : v(x), d(dx) {}
+    explicit operator float() const { return float(v); }
+    explicit operator int() const { return int(v); }
+    Dual& operator+=(const Dual& b) { v += b.v; d += b.d; return *this; }
+    Dual& operator*=(const Dual& b) { d = d * b.v + v * b.d; v *= b.v; return *this; }
+};
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline bool operator<(Dual a, Dual b) { return a.v < b.v; }
+inline bool operator>(Dual a, Dual b) { return a.v > b.v; }
+inline bool operator<=(Dual a, Dual b) { return a.v <= b.v; }
+inline bool operator>=(Dual a, Dual b) { return a.v >= b.v; }
+inline bool operator==(Dual a, Dual b) { return a.v == b.v; }
+inline bool operator!=(Dual a, Dual b) { return a.v != b.v; }
+inline Dual fma_r(Dual a, Dual b, Dual c) { return {std::fma(a.v, b.v, c.v), a.d * b.v + a.v * b.d + c.d}; }
+inline Dual floor_r(Dual a) { return {std::floor(a.v), 0.0}; }
+inline Dual sqrt_r(Dual a) {
+    const double r = std::sqrt(a.v);
+    return {r, r > 0.0 ? a.d / (2.0 * r) : 0.0};
+}
+inline bool isfinite_r(Dual a) { return std::isfinite(a.v); }
+inline Dual fabs_r(Dual a) { return a.v < 0.0 ? -a : a; }
+inline Dual copysign_r(Dual mag, Dual sgn) {
+    const bool flip = std::signbit(mag.v) != std::signbit(sgn.v);
+    return flip ? -mag : mag;
+}
+// s_corr's power: the exponent is a parameter (no derivative taken).
+inline Dual pow_r(Dual a, Dual b) {
+    const double p = std::pow(a.v, b.v);
+    const double dp = (a.v != 0.0) ? b.v * std::pow(a.v, b.v - 1.0) : (b.v == 1.0 ? 1.0 : 0.0);
+    return {p, dp * a.d};
+}
+
+P<Dual> make_p_dual(const pbf_device_params& d, double dxsph_c) {
+    const P<double> q = make_p64(d);
+    P<Dual> p{};
+    p.h = q.h; p.h2 = q.h2; p.poly6 = q.poly6; p.spiky = q.spiky;
+    p.mins = {q.mins.x, q.mins.y, q.mins.z};
+    p.maxs = {q.maxs.x, q.maxs.y, q.maxs.z};
+    p.cs = q.cs;
+    p.dimx = q.dimx; p.dimy = q.dimy; p.dimz = q.dimz;
+    p.g = {q.g.x, q.g.y, q.g.z};
+    p.rest = q.rest; p.dt = q.dt; p.inv_dt = q.inv_dt; p.e = q.e; p.mass = q.mass;
+    p.xsph_c = Dual(q.xsph_c, dxsph_c);
+    p.maxNeighbors = q.maxNeighbors;
+    p.scorr_enable = q.scorr_enable;
+    p.scorr_k = q.scorr_k; p.scorr_n = q.scorr_n; p.scorr_dq_h = q.scorr_dq_h; p.wq_min = q.wq_min;
+    p.scorr_min = q.scorr_min; p.grad_r_eps = q.grad_r_eps; p.lambda_denom_eps = q.lambda_denom_eps;
+    p.compliance = q.compliance;
+    p.enable_lambda_clamp = q.enable_lambda_clamp;
+    p.lambda_max_abs = q.lambda_max_abs;
+    p.enable_disp_clamp = q.enable_disp_clamp;
+    p.disp_clamp_max_h = q.disp_clamp_max_h;
+    p.enable_relax = q.enable_relax;
+    p.relax_omega = q.relax_omega;
+    p.xsph_gate_enable = q.xsph_gate_enable; p.xsph_n_min = q.xsph_n_min; p.xsph_n_max = q.xsph_n_max;
+    return p;
+}
+
 }  // namespace
 
 extern "C" {
@@ -757,6 +845,32 @@ void oracle_density_stats_f32pos(const pbf_sim_params* p, const float4* pos, uin
 
 void oracle_density_stats_f64pos(const pbf_sim_params* p, const double* pos4, uint32_t N, double out[4]) {
     density_stats_impl(*p, pos4, N, out);
+}
+
+int oracle_step_jvp_f64(const pbf_sim_params* p, int hashed, double* pos4, double* vel4, double* dpos4,
+                        double* dvel4, double dxsph_c, uint32_t N, int steps) {
+    pbf_sim_params sp = *p;
+    compute_dims(sp.grid);
+    const pbf_device_params dp = device_params_of(sp);
+    const P<Dual> pd = make_p_dual(dp, dxsph_c);
+    std::vector<V4<Dual>> pos(N), vel(N);
+    for (size_t i = 0; i < N; ++i)
+        for (int c = 0; c < 4; ++c) {
+            (&pos[i].x)[c] = Dual(pos4[4 * i + c], dpos4[4 * i + c]);
+            (&vel[i].x)[c] = Dual(vel4[4 * i + c], dvel4[4 * i + c]);
+        }
+    for (int k = 0; k < steps; ++k) {
+        const int rc = step_t<Dual>(sp, hashed, pos.data(), vel.data(), N, nullptr, pd);
+        if (rc != 0) return rc;
+    }
+    for (size_t i = 0; i < N; ++i)
+        for (int c = 0; c < 4; ++c) {
+            pos4[4 * i + c] = (&pos[i].x)[c].v;
+            dpos4[4 * i + c] = (&pos[i].x)[c].d;
+            vel4[4 * i + c] = (&vel[i].x)[c].v;
+            dvel4[4 * i + c] = (&vel[i].x)[c].d;
+        }
+    return 0;
 }
 
 int oracle_dam_break_params(float bx, float by, float bz, int solver_iters, uint32_t num_particles,

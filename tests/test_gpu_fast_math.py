@@ -1,0 +1,162 @@
+"""PBF_MATH_FAST: the lambda and delta passes with hardware reciprocal square
+roots, reciprocals instead of divisions and (ratio^2)^2 for the s_corr power.
+
+Per step, from the same state, against the FP32 oracle: sorted keys,
+permutation and cell tables bit-exact (they come from the prediction, before
+any neighbour arithmetic); lambda, positions and velocities within the bars of
+tests/parity.py (spec: 1e-5 relative on state).  The single-iteration
+lambda, bit-exact in the exact mode, is held to the same 1e-5 normwise bar.
+"""
+import numpy as np
+import pytest
+
+import pbfx
+from parity import STEP_LAMBDA, STEP_LAMBDA_FLOOR, STEP_POS, assert_velocities_close, step_lambda_tol
+
+pytestmark = pytest.mark.gpu
+
+
+def c1_scene(lib, iters=2):
+    p = pbfx.dam_break_params((1.0, 1.0, 1.0), iters, 32 ** 3)
+    pos = pbfx.seed_lattice(lib, 32, 32, 32, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
+    return p, pos, np.zeros_like(pos)
+
+
+def fast_step_vs_oracle(s, orc, p, hashed):
+    """One fast-mode step of Sim s from its current state, checked against
+    the oracle stepped from the same state."""
+    cur_pos, cur_vel = s.download()
+    opos, ovel = cur_pos.copy(), cur_vel.copy()
+    tr = pbfx.oracle_step(orc, p, hashed, opos, ovel)
+    s.step()
+    np.testing.assert_array_equal(s.fetch(pbfx.DBG_KEYS_SORTED), tr["keys_sorted"])
+    np.testing.assert_array_equal(s.fetch(pbfx.DBG_PERM), tr["perm"])
+    if hashed:
+        m = int(s.fetch(pbfx.DBG_COMPACT_COUNT)[0])
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_UNIQUE_KEYS)[:m], tr["unique_keys"])
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_OFFSETS)[: m + 1], tr["offsets"])
+    else:
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_START), tr["cell_start"])
+        np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_END), tr["cell_end"])
+    gpos, gvel = s.download()
+    if p.solverIters > 0:
+        tol = STEP_LAMBDA if p.solverIters == 1 else step_lambda_tol(p.solverIters)
+        pbfx.assert_close(s.fetch(pbfx.DBG_LAMBDA), tr["lambda"], tol, "lambda", floor_frac=STEP_LAMBDA_FLOOR)
+    pbfx.assert_close(gpos, opos, STEP_POS, "positions")
+    assert_velocities_close(gvel, ovel, opos, p.dt)
+    assert np.all(gpos[:, 3] == 1.0) and np.all(gvel[:, 3] == 0.0)
+
+
+@pytest.mark.parametrize("hashed", [True, False])
+@pytest.mark.parametrize("iters", [1, 2, 4])
+def test_fast_step_from_lattice(gpu, lib, orc, hashed, iters):
+    p, pos, vel = c1_scene(lib, iters)
+    with pbfx.Sim(lib, p, hashed=hashed) as s:
+        s.set_math_mode(pbfx.PBF_MATH_FAST)
+        assert s.math_mode() == pbfx.PBF_MATH_FAST
+        s.upload(pos, vel)
+        fast_step_vs_oracle(s, orc, p, hashed)
+
+
+@pytest.mark.parametrize("hashed", [True, False])
+def test_fast_step_by_step_over_a_run(gpu, lib, orc, hashed):
+    """60 fast steps; every 6th is checked against the oracle from the GPU state."""
+    p, pos, vel = c1_scene(lib)
+    with pbfx.Sim(lib, p, hashed=hashed) as s:
+        s.set_math_mode(pbfx.PBF_MATH_FAST)
+        s.upload(pos, vel)
+        for k in range(60):
+            if k % 6 == 0:
+                fast_step_vs_oracle(s, orc, p, hashed)
+            else:
+                s.step()
+
+
+def test_fast_cap_and_restitution(gpu, lib, orc):
+    """A compressed state with the neighbour cap at 8, restitution 0.5 and
+    random velocities."""
+    p, pos, vel = c1_scene(lib)
+    for _ in range(30):
+        pbfx.oracle_step(orc, p, True, pos, vel, trace=False)
+    p.maxNeighbors = 8
+    p.boundaryRestitution = 0.5
+    rng = np.random.default_rng(5)
+    vel[:, :3] += rng.normal(scale=0.5, size=(pos.shape[0], 3)).astype(np.float32)
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        s.set_math_mode(pbfx.PBF_MATH_FAST)
+        s.upload(pos, vel)
+        fast_step_vs_oracle(s, orc, p, True)
+
+
+@pytest.mark.parametrize("scorr_n", [4.0, 3.0])
+def test_fast_scorr_exponents(gpu, lib, orc, scorr_n):
+    """n = 4 takes the product form, other exponents powf."""
+    p, pos, vel = c1_scene(lib)
+    p.pbf.scorr_n = scorr_n
+    for _ in range(10):
+        pbfx.oracle_step(orc, p, True, pos, vel, trace=False)
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        s.set_math_mode(pbfx.PBF_MATH_FAST)
+        s.upload(pos, vel)
+        fast_step_vs_oracle(s, orc, p, True)
+
+
+def test_fast_c2_in_the_timed_window(gpu, lib, orc):
+    """The bench workload (1,048,576 particles, 2 iterations, hashed): steps 6,
+    15 and 24 of a fast-mode run, each against the oracle from the GPU state."""
+    n = 128 * 64 * 128
+    p = pbfx.dam_break_params((2.0, 1.0, 2.0), 2, n)
+    pos = pbfx.seed_lattice(lib, 128, 64, 128, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC0FFEE, p)
+    with pbfx.Sim(lib, p, hashed=True) as s:
+        s.set_math_mode(pbfx.PBF_MATH_FAST)
+        s.upload(pos, np.zeros_like(pos))
+        for k in range(25):
+            if k in (5, 14, 23):
+                fast_step_vs_oracle(s, orc, p, True)
+            else:
+                s.step()
+
+
+def test_fast_and_exact_modes_switch(gpu, lib):
+    """Switching modes re-captures the step: exact steps after fast ones are
+    the exact path's (bit-identical to a run that never switched)."""
+    p, pos, vel = c1_scene(lib)
+    with pbfx.Sim(lib, p, hashed=True) as a, pbfx.Sim(lib, p, hashed=True) as b:
+        a.upload(pos, vel)
+        b.upload(pos, vel)
+        b.set_math_mode(pbfx.PBF_MATH_FAST)
+        b.step(3)
+        fast_pos, _ = b.download()
+        a.step(3)
+        exact_pos, exact_vel = a.download()
+        assert not np.array_equal(fast_pos, exact_pos)  # different arithmetic
+        pbfx.assert_close(fast_pos, exact_pos, 1e-4, "fast vs exact after 3 steps")
+        b.upload(exact_pos, exact_vel)
+        b.set_math_mode(pbfx.PBF_MATH_EXACT)
+        a.step(2)
+        b.step(2)
+        pa, va = a.download()
+        pb, vb = b.download()
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def test_fast_ensemble_against_oracle(gpu, lib, orc):
+    """Three seeded ensemble scenes (tilted gravity, 3 iterations) in fast mode,
+    every scene checked per step against the oracle."""
+    scenes, pos = pbfx.ensemble_scenes(lib, 3, seed=0xFA57, iters_choices=(3,))
+    with pbfx.Ensemble(lib, scenes) as e:
+        e.set_math_mode(pbfx.PBF_MATH_FAST)
+        e.upload(pos, np.zeros_like(pos))
+        off = e.offsets.astype(np.int64)
+        for k in range(9):
+            cur_pos, cur_vel = e.download()
+            e.step()
+            if k % 4:
+                continue
+            gpos, gvel = e.download()
+            for si, sc in enumerate(scenes):
+                a, b = off[si], off[si + 1]
+                opos, ovel = cur_pos[a:b].copy(), cur_vel[a:b].copy()
+                pbfx.oracle_step(orc, sc, True, opos, ovel, trace=False)
+                pbfx.assert_close(gpos[a:b], opos, STEP_POS, "scene %d positions" % si)
+                assert_velocities_close(gvel[a:b], ovel, opos, sc.dt)
