@@ -100,7 +100,7 @@ struct pbf_ensemble {
              *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr;
     uint32_t nbrCap = 0;
     int tile = 0;  // tile shape of the list passes
-    bool fast = false;  // arithmetic of the lambda / delta passes (PBF_MATH_FAST)
+    bool fast = false;  // arithmetic of the delta pass (PBF_MATH_FAST)
     pbf::SceneInfo* scenes = nullptr;
     void* sortTemp = nullptr;
     size_t sortBytes = 0;

@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
 }
 
 // lambda of iteration `it` for every slot whose scene runs that iteration.
-template <class Scenes, class Sh, bool kFast>
+template <class Scenes, class Sh>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf,
@@ -677,21 +677,21 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
-            a = lambda_queued_acc<kQueue, Sh::kTile, kFast>(active, sc, pi,
+            a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
                                              ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
                                              StagedData{sp, nullptr}, q16);
         else
-            a = lambda_queued_acc<kQueue, Sh::kTile, kFast>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
+            a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
     } else if (staged) {
         int cx, cy, cz;
         decode_key(key_s[sc] - v.cellOffset, dp.grid.dim, cx, cy, cz);
         if (active)
-            a = lambda_of_acc<kFast>(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
+            a = lambda_of_acc(sc, pi, cx, cy, cz, dp, LbRows{lb + v.cellOffset}, [&](uint32_t k, uint32_t& j) {
                 j = k;
                 return __ldg(pred + k);
             });
     } else {
-        a = lambda_queued_acc<kQueue, Sh::kTile, kFast>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
+        a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, row_source(key_s, lb, v, sc), dp, g, q32);
     }
     if (!active) return;
     // the neighbour sums, for the adjoint's replay
@@ -1049,15 +1049,17 @@ cudaError_t with_math(bool fast, F&& f) {
     return fast ? f(std::true_type{}) : f(std::false_type{});
 }
 
-template <class Sh, bool kFast>
+template <class Sh>
 cudaError_t prepare_solve() {
     const int solve = int(Sh::kSolveSmem);
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_lambda<OneScene, Sh, kFast>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_lambda<ManyScenes, Sh, kFast>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<OneScene, Sh, kFast>, a, solve)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_delta<ManyScenes, Sh, kFast>, a, solve)) != cudaSuccess)
+    if ((e = cudaFuncSetAttribute(k_lambda<OneScene, Sh>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_lambda<ManyScenes, Sh>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<OneScene, Sh, false>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<ManyScenes, Sh, false>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<OneScene, Sh, true>, a, solve)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_delta<ManyScenes, Sh, true>, a, solve)) != cudaSuccess)
         return e;
     return cudaSuccess;
 }
@@ -1067,7 +1069,7 @@ cudaError_t prepare_shape() {
     const int commit = int(Sh::kCommitSmem);
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
-    if ((e = prepare_solve<Sh, false>()) != cudaSuccess || (e = prepare_solve<Sh, true>()) != cudaSuccess ||
+    if ((e = prepare_solve<Sh>()) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<OneScene, true, Sh>, a, commit)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<OneScene, false, Sh>, a, commit)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<ManyScenes, true, Sh>, a, commit)) != cudaSuccess)
@@ -1134,7 +1136,7 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
             constexpr bool kFast = decltype(fast)::value;
             const unsigned g = blocks_for(sh.N, Sh::kTile);
             if (which == 0)
-                k_lambda<OneScene, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
+                k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
                     it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh), b.err, b.lambda_acc);
             else
                 k_delta<OneScene, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
@@ -1204,7 +1206,7 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
             constexpr bool kFast = decltype(fast)::value;
             const unsigned g = blocks_for(m.N, Sh::kTile);
             if (which == 0)
-                k_lambda<ManyScenes, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N,
+                k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N,
                                                                                     m.lam_s, lb, m.err, nullptr);
             else
                 k_delta<ManyScenes, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(

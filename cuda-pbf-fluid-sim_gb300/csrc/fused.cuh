@@ -78,8 +78,9 @@ struct FusedShape {
     int list_span;
     // Tile shape of the list passes (0 .. fused_tile_shape_count() - 1).
     int tile;
-    // Arithmetic of the lambda and delta passes: false = exact (bit-identical
-    // to the reference kernels), true = fast (within the 1e-5 bars).
+    // Arithmetic of the delta pass: false = exact (bit-identical to the
+    // reference kernels), true = fast (s_corr power without powf; within the
+    // 1e-5 bars).
     bool fast;
 };
 
@@ -157,7 +158,7 @@ struct MultiBufs {
     uint32_t nbr_cap;  // 0: no lists
     uint32_t* err;     // device error word (kErr* bits)
     int tile;          // tile shape of the list passes
-    bool fast;         // arithmetic of the lambda / delta passes (FusedShape::fast)
+    bool fast;         // arithmetic of the delta pass (FusedShape::fast)
 };
 
 // The list passes of a batch: lists built once from the prediction (for the

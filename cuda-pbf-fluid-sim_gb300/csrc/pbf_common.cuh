@@ -538,49 +538,38 @@ struct CompactRows {
 };
 
 // ------------------------------------------------------- arithmetic modes
-// The neighbour bodies come in two modes (a template flag kFast).
+// The delta pass comes in two modes (a template flag kFast).
 //   exact: the reference kernels' operations with explicit rounding, so
 //          results are bit-identical to the reference's FP32 kernels.
-//   fast:  the same formulas with cheaper operations: r and 1/r from one
-//          hardware reciprocal square root (rsqrtf), 1/max(r, eps) as
-//          min(1/r, 1/eps), multiplications by reciprocals computed once per
-//          walk instead of divisions, the s_corr power for n = 4 as
-//          (ratio^2)^2, |grad|^2 as coeff^2 r^2, and sums contracted into
-//          FMAs.  Each term is within a few ulps of the exact one; per-step
-//          results stay within the 1e-5 relative bars on state.
+//   fast:  the s_corr term without powf: ratio = w * (1 / w_q), with the
+//          reciprocal computed once per walk, and for n = 4 (the default)
+//          ratio^4 = (ratio^2)^2.  Everything else is the exact mode's.  The
+//          power is within ~1.5 ulp of the exact one (CUDA's powf itself is
+//          not correctly rounded), so per-step results stay within the 1e-5
+//          relative bars on state.  A mode that also replaced the correctly
+//          rounded square root and divisions of the spiky gradient by rsqrtf
+//          and reciprocals was measured and dropped: the last iteration's
+//          lambda then left its bar (1.8e-5 at 2 iterations, 1.0e-4 at 4).
 // Constants of the bodies, computed once per walk.
 struct NbrConsts {
-    float inv_eps;  // 1 / grad_r_eps (fast mode)
-    float inv_wq;   // 1 / w_q, 0 when w_q <= 0 (fast mode)
-    float c3s;      // -3 spiky
-    float mpoly6;   // m poly6
+    float inv_wq;  // 1 / w_q, 0 when w_q <= 0 (fast mode)
 };
 
 template <bool kFast>
-__device__ __forceinline__ NbrConsts nbr_consts(const sim::DeviceParams& dp, float w_q) {
+__device__ __forceinline__ NbrConsts nbr_consts(float w_q) {
     NbrConsts c;
-    c.inv_eps = kFast ? 1.0f / dp.pbf.grad_r_eps : 0.f;
-    c.inv_wq = (kFast && w_q > 0.f) ? 1.0f / w_q : 0.f;
-    c.c3s = -3.0f * dp.kernel.spiky;
-    c.mpoly6 = dp.particleMass * dp.kernel.poly6;
+    c.inv_wq = (kFast && w_q > 0.f) ? __fdiv_rn(1.0f, w_q) : 0.f;
     return c;
 }
 
 // Spiky-gradient coefficient -3 spiky (h - r)^2 / max(r, grad_r_eps) of a
 // neighbour at r^2 (sim/pbf_lambda.cu:70-74, sim/pbf_delta_apply.cu:70-74).
-template <bool kFast>
-__device__ __forceinline__ float spiky_coeff(float r2, const sim::DeviceParams& dp, const NbrConsts& c) {
+__device__ __forceinline__ float spiky_coeff(float r2, const sim::DeviceParams& dp) {
     const sim::KernelCoeffs& kc = dp.kernel;
-    if (!kFast) {
-        const float r = sqrt_(r2);
-        const float r_safe = fmaxf(r, dp.pbf.grad_r_eps);
-        const float t = sub_(kc.h, r);
-        return div_(mul_(mul_(-3.0f, kc.spiky), mul_(t, t)), r_safe);
-    }
-    const float ir = rsqrtf(r2);             // +inf at r^2 = 0, where r = 0 below
-    const float r = r2 > 0.f ? r2 * ir : 0.f;
-    const float t = kc.h - r;
-    return c.c3s * (t * t) * fminf(ir, c.inv_eps);
+    const float r = sqrt_(r2);
+    const float r_safe = fmaxf(r, dp.pbf.grad_r_eps);
+    const float t = sub_(kc.h, r);
+    return div_(mul_(mul_(-3.0f, kc.spiky), mul_(t, t)), r_safe);
 }
 
 // ---------------------------------------------------------------- lambda
@@ -593,22 +582,13 @@ struct LambdaAcc {
     uint32_t last = 0;  // candidate index of the last neighbour summed (walks visit them in slot order)
 };
 
-template <bool kFast = false>
 __device__ __forceinline__ void lambda_accumulate(LambdaAcc& a, float rx, float ry, float rz, float r2,
-                                                  const sim::DeviceParams& dp, const NbrConsts& c) {
+                                                  const sim::DeviceParams& dp) {
     const sim::KernelCoeffs& kc = dp.kernel;
     ++a.contrib;
     const float hr2 = sub_(kc.h2, r2);
-    const float coeff = spiky_coeff<kFast>(r2, dp, c);
-    if (kFast) {
-        a.density = fmaf(c.mpoly6 * hr2 * hr2, hr2, a.density);
-        a.gx = fmaf(coeff, rx, a.gx);
-        a.gy = fmaf(coeff, ry, a.gy);
-        a.gz = fmaf(coeff, rz, a.gz);
-        a.sumGrad2 = fmaf(coeff * coeff, r2, a.sumGrad2);  // |coeff r_ij|^2
-        return;
-    }
     a.density = fma_(mul_(mul_(mul_(dp.particleMass, kc.poly6), hr2), hr2), hr2, a.density);
+    const float coeff = spiky_coeff(r2, dp);
     const float ax = mul_(coeff, rx), ay = mul_(coeff, ry), az = mul_(coeff, rz);
     a.gx = add_(a.gx, ax);
     a.gy = add_(a.gy, ay);
@@ -638,11 +618,10 @@ __device__ __forceinline__ float lambda_finalize(const LambdaAcc& a, const sim::
 // Single-pass walk (reference layout): fetch(k, j) returns the candidate's
 // position and writes its identity j (compared with `self`).  *_acc: the
 // neighbour sums before lambda_finalize.
-template <bool kFast = false, class RowRange, class Fetch>
+template <class RowRange, class Fetch>
 __device__ __forceinline__ LambdaAcc lambda_of_acc(uint32_t self, float4 pi, int cx, int cy, int cz,
                                            const sim::DeviceParams& dp, RowRange&& rows, Fetch&& fetch) {
     LambdaAcc a;
-    const NbrConsts c = nbr_consts<kFast>(dp, 0.f);
     const int cap = dp.maxNeighbors;
     const bool hasCap = cap > 0;
     walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
@@ -653,7 +632,7 @@ __device__ __forceinline__ LambdaAcc lambda_of_acc(uint32_t self, float4 pi, int
         float rx, ry, rz;
         const float r2 = dist2(pi, pj, rx, ry, rz);
         if (r2 > dp.kernel.h2) return true;
-        lambda_accumulate<kFast>(a, rx, ry, rz, r2, dp, c);
+        lambda_accumulate(a, rx, ry, rz, r2, dp);
         a.last = j;
         return true;
     });
@@ -670,11 +649,10 @@ __device__ __forceinline__ float lambda_of(uint32_t self, float4 pi, int cx, int
 // RowSource (the stencil) or a ListSource, Data GlobalData or StagedData.
 // Stencil candidates include the particle itself (rejected by slot); lists
 // never do.
-template <int Q, int kStride, bool kFast = false, class Src, class Data, class QT>
+template <int Q, int kStride, class Src, class Data, class QT>
 __device__ __forceinline__ LambdaAcc lambda_queued_acc(bool active, uint32_t s, float4 pi, const Src& src,
                                                const sim::DeviceParams& dp, const Data& data, QT* q) {
     LambdaAcc a;
-    const NbrConsts c = nbr_consts<kFast>(dp, 0.f);
     const int cap = dp.maxNeighbors;
     const float h2 = dp.kernel.h2;
     constexpr bool kSelf = std::is_same<Src, RowSource>::value;
@@ -687,7 +665,7 @@ __device__ __forceinline__ LambdaAcc lambda_queued_acc(bool active, uint32_t s, 
         [&](uint32_t k) {
             float rx, ry, rz;
             const float r2 = dist2(pi, data.p(k), rx, ry, rz);
-            lambda_accumulate<kFast>(a, rx, ry, rz, r2, dp, c);
+            lambda_accumulate(a, rx, ry, rz, r2, dp);
             a.last = k;
         });
     return a;
@@ -712,21 +690,31 @@ __device__ __forceinline__ float scorr_wq(const sim::DeviceParams& dp) {
 // ----------------------------------------------------------------- delta
 // Position correction, sim/pbf_delta_apply.cu:40-112.
 // One neighbour's term (l_ij, a_ij): the sum is d += l_ij * a_ij per axis.
+template <bool kFast = false>
 __device__ __forceinline__ float4 delta_term(float rx, float ry, float rz, float r2, float lam_i, float lam_j,
-                                             float w_q, const sim::DeviceParams& dp) {
+                                             float w_q, const sim::DeviceParams& dp, const NbrConsts& c) {
     const sim::KernelCoeffs& kc = dp.kernel;
     const sim::PbfTuning& pbf = dp.pbf;
-    const float r = sqrt_(r2);
-    const float t = sub_(kc.h, r);
-    const float r_safe = fmaxf(r, pbf.grad_r_eps);
-    const float coeff = div_(mul_(mul_(-3.0f, kc.spiky), mul_(t, t)), r_safe);
+    const float coeff = spiky_coeff(r2, dp);
     const float ax = mul_(coeff, rx), ay = mul_(coeff, ry), az = mul_(coeff, rz);
     float scorr = 0.0f;
     if (pbf.scorr_enable) {
         const float hr2 = sub_(kc.h2, r2);
         const float w = mul_(mul_(mul_(kc.poly6, hr2), hr2), hr2);
-        const float ratio = (w_q > 0.f) ? div_(w, w_q) : 0.0f;
-        scorr = mul_(-pbf.scorr_k, scorr_pow(ratio, pbf.scorr_n));
+        float pw;
+        if (kFast) {
+            const float ratio = mul_(w, c.inv_wq);
+            if (pbf.scorr_n == 4.0f) {
+                const float q = mul_(ratio, ratio);
+                pw = mul_(q, q);
+            } else {
+                pw = powf(ratio, pbf.scorr_n);
+            }
+        } else {
+            const float ratio = (w_q > 0.f) ? div_(w, w_q) : 0.0f;
+            pw = scorr_pow(ratio, pbf.scorr_n);
+        }
+        scorr = mul_(-pbf.scorr_k, pw);
         if (pbf.scorr_min < 0.f) scorr = fmaxf(scorr, pbf.scorr_min);
     }
     return make_float4(add_(add_(lam_i, lam_j), scorr), ax, ay, az);
@@ -742,31 +730,7 @@ template <bool kFast = false>
 __device__ __forceinline__ void delta_accumulate(float3& d, float rx, float ry, float rz, float r2, float lam_i,
                                                  float lam_j, float w_q, const sim::DeviceParams& dp,
                                                  const NbrConsts& c) {
-    if (!kFast) {
-        delta_apply_term(d, delta_term(rx, ry, rz, r2, lam_i, lam_j, w_q, dp));
-        return;
-    }
-    const sim::KernelCoeffs& kc = dp.kernel;
-    const sim::PbfTuning& pbf = dp.pbf;
-    const float coeff = spiky_coeff<true>(r2, dp, c);
-    float scorr = 0.0f;
-    if (pbf.scorr_enable) {
-        const float hr2 = kc.h2 - r2;
-        const float ratio = kc.poly6 * hr2 * hr2 * hr2 * c.inv_wq;
-        float pw;
-        if (pbf.scorr_n == 4.0f) {
-            const float q = ratio * ratio;
-            pw = q * q;
-        } else {
-            pw = powf(ratio, pbf.scorr_n);
-        }
-        scorr = -pbf.scorr_k * pw;
-        if (pbf.scorr_min < 0.f) scorr = fmaxf(scorr, pbf.scorr_min);
-    }
-    const float lc = (lam_i + lam_j + scorr) * coeff;
-    d.x = fmaf(lc, rx, d.x);
-    d.y = fmaf(lc, ry, d.y);
-    d.z = fmaf(lc, rz, d.z);
+    delta_apply_term(d, delta_term<kFast>(rx, ry, rz, r2, lam_i, lam_j, w_q, dp, c));
 }
 
 __device__ __forceinline__ float3 delta_finalize(float3 dsum, const sim::DeviceParams& dp) {
@@ -799,7 +763,7 @@ template <bool kFast = false, class RowRange, class Fetch>
 __device__ __forceinline__ float3 delta_of_sum(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
                                            const sim::DeviceParams& dp, float w_q, RowRange&& rows, Fetch&& fetch) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
-    const NbrConsts c = nbr_consts<kFast>(dp, w_q);
+    const NbrConsts c = nbr_consts<kFast>(w_q);
     walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
         uint32_t j;
         float lam_j;
@@ -824,7 +788,7 @@ template <int Q, int kStride, bool kFast = false, class Src, class Data, class Q
 __device__ __forceinline__ float3 delta_queued_sum(bool active, uint32_t s, float4 pi, float lam_i, const Src& src,
                                                const sim::DeviceParams& dp, float w_q, const Data& data, QT* q) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
-    const NbrConsts c = nbr_consts<kFast>(dp, w_q);
+    const NbrConsts c = nbr_consts<kFast>(w_q);
     const float h2 = dp.kernel.h2;
     constexpr bool kSelf = std::is_same<Src, RowSource>::value;
     walk_source<Q, kStride, false>(

@@ -215,7 +215,7 @@ _ORACLE_SIGS = {
     "oracle_step_f64": ([C.POINTER(SimParams), _I, _VP, _VP, _U32], _I),
     "oracle_density_stats_f32pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
     "oracle_density_stats_f64pos": ([C.POINTER(SimParams), _VP, _U32, C.POINTER(C.c_double * 4)], None),
-    "oracle_step_jvp_f64": ([C.POINTER(SimParams), _I, _VP, _VP, _VP, _VP, C.c_double, _U32, _I], _I),
+    "oracle_step_jvp": ([C.POINTER(SimParams), _I, _I, _VP, _VP, _VP, _VP, C.c_double, _U32, _I], _I),
     "oracle_dam_break_params": ([_F, _F, _F, _I, _U32, C.POINTER(SimParams)], _I),
     "oracle_seed_lattice": ([_VP, _U32, _U32, _U32, _F, _F, _F, _F, _F, C.c_uint64, C.POINTER(GridBounds)], None),
 }

@@ -13,6 +13,15 @@
 //   d_lambda            lambda in cell order
 //   grid: d_cellKeys (id order), d_cellKeys_sorted, d_indices_sorted (sorted
 //   slot -> original id), d_cellLowerBound (numCells+1), compact table.
+//
+// For launchers registered through KernelDispatcher (KernelLaunchFn): the
+// names are the reference's but the layout is not.  A launcher written
+// against the reference's sim/device_buffers.cuh reads d_pos_pred and
+// d_lambda by particle id; here they are indexed by sorted slot s, whose
+// particle is d_indices_sorted[s].  d_delta, d_pos_curr and d_pos_next do not
+// exist: the Jacobi update ping-pongs between d_pos_pred and d_pred_alt
+// (SolvedPrediction below gives the last one) and the commit writes d_pos /
+// d_vel in place.  tests/cpp/plugin_path.cu is a worked example.
 #pragma once
 
 #include <cstddef>
@@ -46,8 +55,8 @@ struct DeviceBuffers {
     // Tile shape of the list passes (particles per CTA and staged slots; the
     // results do not depend on it).
     int tileShape = 0;
-    // Arithmetic of the lambda and delta passes: 0 exact (bit-identical to
-    // the reference kernels), 1 fast (within the 1e-5 bars; PBF_MATH_FAST).
+    // Arithmetic of the delta pass: 0 exact (bit-identical to the reference
+    // kernels), 1 fast (within the 1e-5 bars; PBF_MATH_FAST).
     int mathMode = 0;
 
     bool allocate(uint32_t cap);
@@ -83,6 +92,13 @@ struct GridBuffers {
     void release();
     ~GridBuffers() { release(); }
 };
+
+// The prediction the last solver iteration wrote (cell order), i.e. the
+// input of the Post phase: iteration `it` reads d_pos_pred when it is even
+// and writes d_pred_alt, and the other way round when it is odd.
+inline float4* SolvedPrediction(const DeviceBuffers& b, int solverIters) {
+    return (solverIters % 2 == 0) ? b.d_pos_pred : b.d_pred_alt;
+}
 
 class KernelDispatcher;
 

@@ -284,16 +284,16 @@ int pbf_get_tile_shape(pbf_sim* sim, int* id);
  * NULL) the selected shape.  Synchronous. */
 int pbf_autotune_tile_shape(pbf_sim* sim, const pbf_sim_params* p, int steps, float* ms, int* chosen);
 
-/* Arithmetic of the lambda and delta passes (no counterpart in the
- * reference).  PBF_MATH_EXACT (the default) evaluates the reference kernels'
- * operations with their rounding: keys, permutation, cell tables, lambda,
- * positions and velocities are bit-identical to the reference's FP32 kernels.
- * PBF_MATH_FAST evaluates the same formulas with the GPU's reciprocal square
- * root (r and 1/r from one rsqrtf), multiplications by reciprocals instead of
- * divisions, (ratio^2)^2 for the s_corr power with n = 4 and contracted
- * sums: keys, permutation and cell tables of a step stay bit-exact, lambda,
- * positions and velocities agree with the exact mode within 1e-5 relative per
- * step.  Takes effect at the next step. */
+/* Arithmetic of the delta pass (no counterpart in the reference).
+ * PBF_MATH_EXACT (the default) evaluates the reference kernels' operations
+ * with their rounding: keys, permutation, cell tables, lambda, positions and
+ * velocities are bit-identical to the reference's FP32 kernels.
+ * PBF_MATH_FAST evaluates the s_corr term without powf: the ratio w / w_q as
+ * a product with 1 / w_q, and for the default exponent n = 4 the power as
+ * (ratio^2)^2.  Everything else is the exact mode's: keys, permutation,
+ * cell tables and the first iteration's lambda stay bit-exact; lambda,
+ * positions and velocities agree with the exact mode within 1e-5 relative
+ * per step.  Takes effect at the next step. */
 enum { PBF_MATH_EXACT = 0, PBF_MATH_FAST = 1 };
 int pbf_set_math_mode(pbf_sim* sim, int mode);
 int pbf_get_math_mode(pbf_sim* sim, int* mode);
@@ -353,8 +353,8 @@ int pbf_ensemble_launches_per_step(pbf_ensemble* ens);
  * fastest shape kept (the step graph is re-captured for it). */
 int pbf_ensemble_set_tile_shape(pbf_ensemble* ens, int id);
 int pbf_ensemble_get_tile_shape(pbf_ensemble* ens, int* id);
-/* Arithmetic mode of the ensemble's lambda and delta passes (see
- * pbf_set_math_mode); the step graph is captured again. */
+/* Arithmetic mode of the ensemble's delta pass (see pbf_set_math_mode);
+ * the step graph is captured again. */
 int pbf_ensemble_set_math_mode(pbf_ensemble* ens, int mode);
 int pbf_ensemble_get_math_mode(pbf_ensemble* ens, int* mode);
 int pbf_ensemble_autotune(pbf_ensemble* ens, int steps, float* ms, int* chosen);

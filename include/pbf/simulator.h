@@ -135,11 +135,10 @@ public:
     // depends on the scene.  setTileShape takes effect at the next step.
     bool setTileShape(int id);
     int tileShape() const { return m_bufs.tileShape; }
-    // Arithmetic of the lambda and delta passes: 0 exact (the default;
-    // bit-identical to the reference kernels), 1 fast (the same formulas with
-    // hardware reciprocal square roots, reciprocals and products for the
-    // s_corr power; per-step state within 1e-5 relative).  Takes effect at
-    // the next step (the step graph is captured again).
+    // Arithmetic of the delta pass: 0 exact (the default; bit-identical to
+    // the reference kernels), 1 fast (the s_corr power as products instead of
+    // powf; per-step state within 1e-5 relative).  Takes effect at the next
+    // step (the step graph is captured again).
     bool setMathMode(int mode);
     int mathMode() const { return m_bufs.mathMode; }
     // Times `steps` steps of every tile shape from the current state (after

@@ -680,75 +680,123 @@ void density_stats_impl(const pbf_sim_params& sp0, const double* xyz4, uint32_t 
 }
 
 // ----------------------------------------------- forward-mode derivative
-// Dual numbers v + d e (e^2 = 0) in FP64: running the step on them carries the
-// exact directional derivative of the FP64 step beside its value, with every
-// branch (neighbour sets, clamps, caps, boundary) decided by the values, as
-// the step itself decides it.  This is the FP64 reference the adjoint's
-// vector-Jacobian products are checked against.
-struct Dual {
-    double v, d;
-    Dual() = default;
-    Dual(double x) : v(x), d(0.0) {}  // NOLINT: constants and FP32 parameters
-    Dual(double x, double dx) : v(x), d(dx) {}
+// Dual numbers v + d e (e^2 = 0): running the step on them carries the exact
+// directional derivative beside the value, with every branch (neighbour
+// sets, caps, clamps, boundary) decided by the values, as the step itself
+// decides it.  The derivative part is always FP64.  The value part is either
+// FP64 (the derivative of the FP64 step) or FP32 (V = float: the values are
+// the FP32 oracle's, i.e. the trajectory the GPU computes, up to the s_corr
+// powf ulps, and the derivative is the FP64-accurate derivative along it,
+// the reference tape of the adjoint's vector-Jacobian products).
+template <class V>
+struct DualT {
+    V v;
+    double d;
+    DualT() = default;
+    DualT(double x) : v(V(x)), d(0.0) {}  // NOLINT: constants and parameters
+    DualT(V x, double dx, int) : v(x), d(dx) {}
     explicit operator float() const { return float(v); }
     explicit operator int() const { return int(v); }
-    Dual& operator+=(const Dual& b) { v += b.v; d += b.d; return *this; }
-    Dual& operator*=(const Dual& b) { d = d * b.v + v * b.d; v *= b.v; return *this; }
+    DualT& operator+=(const DualT& b) { v = v + b.v; d += b.d; return *this; }
+    DualT& operator*=(const DualT& b) { d = d * double(b.v) + double(v) * b.d; v = v * b.v; return *this; }
 };
-inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
-inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
-inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
-inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
-inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
-inline bool operator<(Dual a, Dual b) { return a.v < b.v; }
-inline bool operator>(Dual a, Dual b) { return a.v > b.v; }
-inline bool operator<=(Dual a, Dual b) { return a.v <= b.v; }
-inline bool operator>=(Dual a, Dual b) { return a.v >= b.v; }
-inline bool operator==(Dual a, Dual b) { return a.v == b.v; }
-inline bool operator!=(Dual a, Dual b) { return a.v != b.v; }
-inline Dual fma_r(Dual a, Dual b, Dual c) { return {std::fma(a.v, b.v, c.v), a.d * b.v + a.v * b.d + c.d}; }
-inline Dual floor_r(Dual a) { return {std::floor(a.v), 0.0}; }
-inline Dual sqrt_r(Dual a) {
-    const double r = std::sqrt(a.v);
-    return {r, r > 0.0 ? a.d / (2.0 * r) : 0.0};
+template <class V> inline DualT<V> mk(V v, double d) { return DualT<V>(v, d, 0); }
+template <class V> inline DualT<V> operator+(DualT<V> a, DualT<V> b) { return mk<V>(a.v + b.v, a.d + b.d); }
+template <class V> inline DualT<V> operator-(DualT<V> a, DualT<V> b) { return mk<V>(a.v - b.v, a.d - b.d); }
+template <class V> inline DualT<V> operator-(DualT<V> a) { return mk<V>(-a.v, -a.d); }
+template <class V> inline DualT<V> operator*(DualT<V> a, DualT<V> b) {
+    return mk<V>(a.v * b.v, a.d * double(b.v) + double(a.v) * b.d);
 }
-inline bool isfinite_r(Dual a) { return std::isfinite(a.v); }
-inline Dual fabs_r(Dual a) { return a.v < 0.0 ? -a : a; }
-inline Dual copysign_r(Dual mag, Dual sgn) {
-    const bool flip = std::signbit(mag.v) != std::signbit(sgn.v);
-    return flip ? -mag : mag;
+template <class V> inline DualT<V> operator/(DualT<V> a, DualT<V> b) {
+    const double bv = double(b.v);
+    return mk<V>(a.v / b.v, (a.d * bv - double(a.v) * b.d) / (bv * bv));
+}
+template <class V> inline bool operator<(DualT<V> a, DualT<V> b) { return a.v < b.v; }
+template <class V> inline bool operator>(DualT<V> a, DualT<V> b) { return a.v > b.v; }
+template <class V> inline bool operator<=(DualT<V> a, DualT<V> b) { return a.v <= b.v; }
+template <class V> inline bool operator>=(DualT<V> a, DualT<V> b) { return a.v >= b.v; }
+template <class V> inline bool operator==(DualT<V> a, DualT<V> b) { return a.v == b.v; }
+template <class V> inline bool operator!=(DualT<V> a, DualT<V> b) { return a.v != b.v; }
+template <class V> inline DualT<V> fma_r(DualT<V> a, DualT<V> b, DualT<V> c) {
+    return mk<V>(fma_r(a.v, b.v, c.v), a.d * double(b.v) + double(a.v) * b.d + c.d);
+}
+template <class V> inline DualT<V> floor_r(DualT<V> a) { return mk<V>(floor_r(a.v), 0.0); }
+template <class V> inline DualT<V> sqrt_r(DualT<V> a) {
+    const V r = sqrt_r(a.v);
+    return mk<V>(r, r > V(0) ? a.d / (2.0 * double(r)) : 0.0);
+}
+template <class V> inline bool isfinite_r(DualT<V> a) { return isfinite_r(a.v); }
+template <class V> inline DualT<V> fabs_r(DualT<V> a) { return a.v < V(0) ? -a : a; }
+template <class V> inline DualT<V> copysign_r(DualT<V> mag, DualT<V> sgn) {
+    return std::signbit(mag.v) != std::signbit(sgn.v) ? -mag : mag;
 }
 // s_corr's power: the exponent is a parameter (no derivative taken).
-inline Dual pow_r(Dual a, Dual b) {
-    const double p = std::pow(a.v, b.v);
-    const double dp = (a.v != 0.0) ? b.v * std::pow(a.v, b.v - 1.0) : (b.v == 1.0 ? 1.0 : 0.0);
-    return {p, dp * a.d};
+template <class V> inline DualT<V> pow_r(DualT<V> a, DualT<V> b) {
+    const double av = double(a.v), bv = double(b.v);
+    const double dp = (av != 0.0) ? bv * std::pow(av, bv - 1.0) : (bv == 1.0 ? 1.0 : 0.0);
+    return mk<V>(pow_r(a.v, b.v), dp * a.d);
 }
 
-P<Dual> make_p_dual(const pbf_device_params& d, double dxsph_c) {
-    const P<double> q = make_p64(d);
-    P<Dual> p{};
-    p.h = q.h; p.h2 = q.h2; p.poly6 = q.poly6; p.spiky = q.spiky;
-    p.mins = {q.mins.x, q.mins.y, q.mins.z};
-    p.maxs = {q.maxs.x, q.maxs.y, q.maxs.z};
-    p.cs = q.cs;
+// Parameters of the dual step: the FP64 oracle's (kernel constants recomputed
+// in double) or the FP32 oracle's, with the direction's component along
+// xsph_c.
+template <class V>
+P<DualT<V>> make_p_dual(const pbf_device_params& d, double dxsph_c) {
+    using D = DualT<V>;
+    P<V> q;
+    if constexpr (sizeof(V) == 8)
+        q = make_p64(d);
+    else
+        q = make_p<float>(d);
+    P<D> p{};
+    auto c = [](V x) { return mk<V>(x, 0.0); };
+    p.h = c(q.h); p.h2 = c(q.h2); p.poly6 = c(q.poly6); p.spiky = c(q.spiky);
+    p.mins = {c(q.mins.x), c(q.mins.y), c(q.mins.z)};
+    p.maxs = {c(q.maxs.x), c(q.maxs.y), c(q.maxs.z)};
+    p.cs = c(q.cs);
     p.dimx = q.dimx; p.dimy = q.dimy; p.dimz = q.dimz;
-    p.g = {q.g.x, q.g.y, q.g.z};
-    p.rest = q.rest; p.dt = q.dt; p.inv_dt = q.inv_dt; p.e = q.e; p.mass = q.mass;
-    p.xsph_c = Dual(q.xsph_c, dxsph_c);
+    p.g = {c(q.g.x), c(q.g.y), c(q.g.z)};
+    p.rest = c(q.rest); p.dt = c(q.dt); p.inv_dt = c(q.inv_dt); p.e = c(q.e); p.mass = c(q.mass);
+    p.xsph_c = mk<V>(q.xsph_c, dxsph_c);
     p.maxNeighbors = q.maxNeighbors;
     p.scorr_enable = q.scorr_enable;
-    p.scorr_k = q.scorr_k; p.scorr_n = q.scorr_n; p.scorr_dq_h = q.scorr_dq_h; p.wq_min = q.wq_min;
-    p.scorr_min = q.scorr_min; p.grad_r_eps = q.grad_r_eps; p.lambda_denom_eps = q.lambda_denom_eps;
-    p.compliance = q.compliance;
+    p.scorr_k = c(q.scorr_k); p.scorr_n = c(q.scorr_n); p.scorr_dq_h = c(q.scorr_dq_h); p.wq_min = c(q.wq_min);
+    p.scorr_min = c(q.scorr_min); p.grad_r_eps = c(q.grad_r_eps); p.lambda_denom_eps = c(q.lambda_denom_eps);
+    p.compliance = c(q.compliance);
     p.enable_lambda_clamp = q.enable_lambda_clamp;
-    p.lambda_max_abs = q.lambda_max_abs;
+    p.lambda_max_abs = c(q.lambda_max_abs);
     p.enable_disp_clamp = q.enable_disp_clamp;
-    p.disp_clamp_max_h = q.disp_clamp_max_h;
+    p.disp_clamp_max_h = c(q.disp_clamp_max_h);
     p.enable_relax = q.enable_relax;
-    p.relax_omega = q.relax_omega;
+    p.relax_omega = c(q.relax_omega);
     p.xsph_gate_enable = q.xsph_gate_enable; p.xsph_n_min = q.xsph_n_min; p.xsph_n_max = q.xsph_n_max;
     return p;
+}
+
+template <class V>
+int step_jvp(const pbf_sim_params& sp, int hashed, double* pos4, double* vel4, double* dpos4, double* dvel4,
+             double dxsph_c, uint32_t N, int steps) {
+    using D = DualT<V>;
+    const pbf_device_params dp = device_params_of(sp);
+    const P<D> pd = make_p_dual<V>(dp, dxsph_c);
+    std::vector<V4<D>> pos(N), vel(N);
+    for (size_t i = 0; i < N; ++i)
+        for (int c = 0; c < 4; ++c) {
+            (&pos[i].x)[c] = mk<V>(V(pos4[4 * i + c]), dpos4[4 * i + c]);
+            (&vel[i].x)[c] = mk<V>(V(vel4[4 * i + c]), dvel4[4 * i + c]);
+        }
+    for (int k = 0; k < steps; ++k) {
+        const int rc = step_t<D>(sp, hashed, pos.data(), vel.data(), N, nullptr, pd);
+        if (rc != 0) return rc;
+    }
+    for (size_t i = 0; i < N; ++i)
+        for (int c = 0; c < 4; ++c) {
+            pos4[4 * i + c] = double((&pos[i].x)[c].v);
+            dpos4[4 * i + c] = (&pos[i].x)[c].d;
+            vel4[4 * i + c] = double((&vel[i].x)[c].v);
+            dvel4[4 * i + c] = (&vel[i].x)[c].d;
+        }
+    return 0;
 }
 
 }  // namespace
@@ -847,30 +895,12 @@ void oracle_density_stats_f64pos(const pbf_sim_params* p, const double* pos4, ui
     density_stats_impl(*p, pos4, N, out);
 }
 
-int oracle_step_jvp_f64(const pbf_sim_params* p, int hashed, double* pos4, double* vel4, double* dpos4,
-                        double* dvel4, double dxsph_c, uint32_t N, int steps) {
+int oracle_step_jvp(const pbf_sim_params* p, int hashed, int fp32_values, double* pos4, double* vel4,
+                    double* dpos4, double* dvel4, double dxsph_c, uint32_t N, int steps) {
     pbf_sim_params sp = *p;
     compute_dims(sp.grid);
-    const pbf_device_params dp = device_params_of(sp);
-    const P<Dual> pd = make_p_dual(dp, dxsph_c);
-    std::vector<V4<Dual>> pos(N), vel(N);
-    for (size_t i = 0; i < N; ++i)
-        for (int c = 0; c < 4; ++c) {
-            (&pos[i].x)[c] = Dual(pos4[4 * i + c], dpos4[4 * i + c]);
-            (&vel[i].x)[c] = Dual(vel4[4 * i + c], dvel4[4 * i + c]);
-        }
-    for (int k = 0; k < steps; ++k) {
-        const int rc = step_t<Dual>(sp, hashed, pos.data(), vel.data(), N, nullptr, pd);
-        if (rc != 0) return rc;
-    }
-    for (size_t i = 0; i < N; ++i)
-        for (int c = 0; c < 4; ++c) {
-            pos4[4 * i + c] = (&pos[i].x)[c].v;
-            dpos4[4 * i + c] = (&pos[i].x)[c].d;
-            vel4[4 * i + c] = (&vel[i].x)[c].v;
-            dvel4[4 * i + c] = (&vel[i].x)[c].d;
-        }
-    return 0;
+    return fp32_values ? step_jvp<float>(sp, hashed, pos4, vel4, dpos4, dvel4, dxsph_c, N, steps)
+                       : step_jvp<double>(sp, hashed, pos4, vel4, dpos4, dvel4, dxsph_c, N, steps);
 }
 
 int oracle_dam_break_params(float bx, float by, float bz, int solver_iters, uint32_t num_particles,

@@ -104,14 +104,18 @@ void oracle_density_stats_f32pos(const pbf_sim_params* p, const float4* pos,
 void oracle_density_stats_f64pos(const pbf_sim_params* p, const double* pos4,
                                  uint32_t N, double out[4]);
 
-/* FP64 steps differentiated in forward mode (dual numbers): pos4/vel4
- * (double[4N], xyzw) are advanced `steps` steps in place, and the direction
- * (dpos4, dvel4, dxsph_c) of the initial state is carried along, so that on
- * return dpos4/dvel4 hold the directional derivative of the final state.
- * Branches (neighbour sets, caps, clamps, boundary) follow the values.
- * The FP64 reference of the adjoint's vector-Jacobian products. */
-int oracle_step_jvp_f64(const pbf_sim_params* p, int hashed, double* pos4, double* vel4,
-                        double* dpos4, double* dvel4, double dxsph_c, uint32_t N, int steps);
+/* Steps differentiated in forward mode (dual numbers, derivative part in
+ * FP64): pos4/vel4 (double[4N], xyzw) are advanced `steps` steps in place, and
+ * the direction (dpos4, dvel4, dxsph_c) of the initial state is carried
+ * along, so that on return dpos4/dvel4 hold the directional derivative of the
+ * final state.  Branches (neighbour sets, caps, clamps, boundary) follow the
+ * values.  fp32_values = 0: the values are the FP64 step's; 1: the values are
+ * the FP32 oracle step's (pos4/vel4 then hold floats), so the derivative is
+ * taken along the FP32 trajectory the GPU computes - the reference tape of
+ * the adjoint's vector-Jacobian products. */
+int oracle_step_jvp(const pbf_sim_params* p, int hashed, int fp32_values, double* pos4,
+                    double* vel4, double* dpos4, double* dvel4, double dxsph_c, uint32_t N,
+                    int steps);
 
 /* Scene generation for the CPU arm, so that it needs no product library.
  * The dam-break parameters: particle radius 0.005 m, spacing 2r, h = 2.5 r

@@ -1,19 +1,25 @@
-"""The adjoint's vector-Jacobian products against an FP64 reference.
+"""The adjoint's vector-Jacobian products against an FP64 reference tape.
 
 pbf_backward differentiates the recorded steps in reverse (neighbour sets
 held fixed within a step, clamps passing the derivative of the branch
-taken).  The reference here is the FP64 oracle step run on dual numbers
-(oracle_step_jvp_f64): it carries the exact directional derivative of the
-FP64 step beside its value, through the same branches.  For cotangents
-(pbar, vbar) of the final state and a unit direction e_k of the initial state
-(one position or velocity coordinate, or xsph_c), the adjoint's k-th gradient
+taken).  The reference here is the oracle step run on dual numbers
+(oracle_step_jvp) with FP32 values and FP64 derivatives: the values follow
+the FP32 trajectory the GPU computes (the FP32 oracle's arithmetic, checked
+bit-identical below), and beside them it carries the directional derivative
+of that step in FP64, through the same branches.  For cotangents (pbar, vbar)
+of the final state and a unit direction e_k of the initial state (one
+position or velocity coordinate, or xsph_c), the adjoint's k-th gradient
 entry must equal pbar . dx_T + vbar . dv_T of the forward derivative.
 
-Unlike differences of a long rollout, this is well conditioned at the
-reference's default constants (s_corr on, the displacement clamp engaged
-for most particles): C1-size scenes (32,768 particles), one and three steps
-from a state 10 steps into the dam break, 49 position, 49 velocity
-coordinates and xsph_c, held to 1e-3 of the largest checked entry.
+Unlike differences of a rollout, this is well conditioned at the reference's
+default constants (s_corr on, the displacement clamp engaged for most
+particles): C1-size scenes (32,768 particles), one and three steps from a
+state 10 steps into the dam break, 49 position and 49 velocity coordinates
+(40 random, 9 of the largest entries) and xsph_c, held to 1e-3 of the
+largest checked entry.  (With FP64 values the tape would follow the FP64
+trajectory, which leaves the FP32 one by ~3e-7 m per step in this chaotic
+regime; its derivatives then differ from the FP32 step's by ~1e-3 after one
+step and by tens of percent after three.)
 """
 import ctypes as C
 
@@ -57,8 +63,9 @@ def adjoint(gpu, lib, p, pos, vel, pbar, vbar, steps):
 
 
 def fp64_directional(orc, p, pos, vel, pbar, vbar, steps, which, i=0, a=0):
-    """pbar . dx_T + vbar . dv_T for the unit direction: which = 'pos' / 'vel'
-    (coordinate a of particle i) or 'xsph_c'."""
+    """pbar . dx_T + vbar . dv_T along the FP32 trajectory, for the unit
+    direction: which = 'pos' / 'vel' (coordinate a of particle i) or
+    'xsph_c'."""
     x = np.ascontiguousarray(pos, np.float64)
     v = np.ascontiguousarray(vel, np.float64)
     dx, dv = np.zeros_like(x), np.zeros_like(v)
@@ -69,23 +76,33 @@ def fp64_directional(orc, p, pos, vel, pbar, vbar, steps, which, i=0, a=0):
         dv[i, a] = 1.0
     else:
         dc = 1.0
-    rc = orc.oracle_step_jvp_f64(C.byref(p), 1, pbfx.ptr(x), pbfx.ptr(v), pbfx.ptr(dx), pbfx.ptr(dv), dc,
-                                 x.shape[0], steps)
+    rc = orc.oracle_step_jvp(C.byref(p), 1, 1, pbfx.ptr(x), pbfx.ptr(v), pbfx.ptr(dx), pbfx.ptr(dv), dc,
+                             x.shape[0], steps)
     assert rc == 0
     return float(np.sum(pbar[:, :3] * dx[:, :3]) + np.sum(vbar[:, :3] * dv[:, :3]))
 
 
-def test_dual_step_value_is_the_fp64_step(lib, orc):
-    """The dual-number step's value part is the FP64 oracle's step."""
+@pytest.mark.parametrize("fp32_values", [1, 0])
+def test_dual_step_values_are_the_oracle_steps(lib, orc, fp32_values):
+    """The dual-number step's value part is the FP32 oracle step (fp32_values
+    = 1) or the FP64 oracle step (0), bit for bit, over two steps."""
     p, pos, vel = c1_state(lib, orc)
     x, v = np.ascontiguousarray(pos, np.float64), np.ascontiguousarray(vel, np.float64)
-    x2, v2 = x.copy(), v.copy()
     dx, dv = np.zeros_like(x), np.zeros_like(v)
-    assert orc.oracle_step_jvp_f64(C.byref(p), 1, pbfx.ptr(x), pbfx.ptr(v), pbfx.ptr(dx), pbfx.ptr(dv), 0.0,
-                                   x.shape[0], 1) == 0
-    assert orc.oracle_step_f64(C.byref(p), 1, pbfx.ptr(x2), pbfx.ptr(v2), x2.shape[0]) == 0
-    np.testing.assert_array_equal(x, x2)
-    np.testing.assert_array_equal(v, v2)
+    assert orc.oracle_step_jvp(C.byref(p), 1, fp32_values, pbfx.ptr(x), pbfx.ptr(v), pbfx.ptr(dx), pbfx.ptr(dv),
+                               0.0, x.shape[0], 2) == 0
+    if fp32_values:
+        x2, v2 = pos.copy(), vel.copy()
+        for _ in range(2):
+            pbfx.oracle_step(orc, p, True, x2, v2, trace=False)
+        np.testing.assert_array_equal(x.astype(np.float32), x2)
+        np.testing.assert_array_equal(v.astype(np.float32), v2)
+    else:
+        x2, v2 = np.ascontiguousarray(pos, np.float64), np.ascontiguousarray(vel, np.float64)
+        for _ in range(2):
+            assert orc.oracle_step_f64(C.byref(p), 1, pbfx.ptr(x2), pbfx.ptr(v2), x2.shape[0]) == 0
+        np.testing.assert_array_equal(x, x2)
+        np.testing.assert_array_equal(v, v2)
     assert not dx.any() and not dv.any()
 
 

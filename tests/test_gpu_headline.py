@@ -65,9 +65,11 @@ def test_c2_fused_step_is_bit_identical_to_reference_kernels(gpu, lib, hashed):
     assert checked == [1, 10, 20]
 
 
-def oracle_compare_step(s, orc, p, hashed, pos_floor=0.01):
+def oracle_compare_step(s, orc, p, hashed, pos_floor=0.01, lam_tol=None):
     """One GPU step checked against the oracle stepped from the GPU's state.
-    pos_floor: the positions' relative-error floor as a fraction of max|x|."""
+    pos_floor: the positions' relative-error floor as a fraction of max|x|;
+    lam_tol: the last iteration's lambda bar (normwise), default the
+    iteration-scaled bar of tests/parity.py."""
     cur_pos, cur_vel = s.download()
     opos, ovel = cur_pos.copy(), cur_vel.copy()
     tr = pbfx.oracle_step(orc, p, hashed, opos, ovel)
@@ -82,7 +84,7 @@ def oracle_compare_step(s, orc, p, hashed, pos_floor=0.01):
         np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_START), tr["cell_start"])
         np.testing.assert_array_equal(s.fetch(pbfx.DBG_CELL_END), tr["cell_end"])
     gpos, gvel = s.download()
-    pbfx.assert_close(s.fetch(pbfx.DBG_LAMBDA), tr["lambda"], step_lambda_tol(p.solverIters), "lambda",
+    pbfx.assert_close(s.fetch(pbfx.DBG_LAMBDA), tr["lambda"], lam_tol or step_lambda_tol(p.solverIters), "lambda",
                       floor_frac=STEP_LAMBDA_FLOOR)
     pbfx.assert_close(gpos, opos, STEP_POS, "positions", floor_frac=pos_floor)
     assert_velocities_close(gvel, ovel, opos, p.dt)
@@ -128,20 +130,23 @@ def test_c3_slice_bit_identical_to_reference_kernels(gpu, lib):
 
 def test_c3_slice_against_oracle(gpu, lib, orc):
     """C3 steps 21..25, each against the oracle stepped from the GPU's state:
-    keys, permutation and cell tables bit-exact, lambda at its bar.  The
-    oracle's s_corr power is the C library's powf; the reference's (and this
-    library's) is CUDA's, which is not correctly rounded.  Over 4 iterations
-    of this pile-up those ulps compound to ~1e-6 m in a few particles, so the
-    positions are held to 1e-5 relative to the scene's extent (normwise) here;
-    the per-coordinate bar with its 1% floor holds at 2 iterations (C2) and
-    the reference kernels agree bit for bit (previous test)."""
+    keys, permutation and cell tables bit-exact.  The oracle's s_corr power is
+    the C library's powf; the reference's (and this library's) is CUDA's,
+    which is not correctly rounded.  Over 4 iterations of this pile-up those
+    ulps compound: positions are held to 1e-5 relative to the scene's extent
+    (normwise; ~1e-6 m apart in a few particles, which the per-coordinate bar
+    with its 1% floor does not allow), and the last iteration's lambda to 1e-3
+    normwise (1.3e-4 measured; lambda = -C/denom of a pile compressed far past
+    rest density amplifies a position ulp).  The per-coordinate bars hold at 2
+    iterations (C2), and the reference kernels agree bit for bit at C3
+    (previous test)."""
     cfg, p, pos, vel = c3_scene(lib)
     with pbfx.Sim(lib, p, hashed=True) as s:
         s.set_list_capacity(cfg["list_capacity"])
         s.upload(pos, vel)
         s.step(20)
         for _ in range(5):
-            oracle_compare_step(s, orc, p, hashed=True, pos_floor=1.0)
+            oracle_compare_step(s, orc, p, hashed=True, pos_floor=1.0, lam_tol=1e-3)
 
 
 def test_c4_scenes_against_oracle(gpu, lib, orc):
