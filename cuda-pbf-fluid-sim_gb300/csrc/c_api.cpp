@@ -581,7 +581,7 @@ int pbf_debug_fetch(pbf_sim* h, int item, void* dst, size_t bytes) {
 
 int pbf_debug_eval_math(int fn, const float* a, const float* b, float* out, uint32_t n) {
     if (n == 0) return PBF_OK;
-    if (!a || !out || (fn != 1 && !b) || fn < 0 || fn > 2) return PBF_ERR_INVALID;
+    if (!a || !out || (fn != 1 && fn != 3 && !b) || fn < 0 || fn > 3) return PBF_ERR_INVALID;
     cudaError_t e = pbf::eval_math(fn, a, b, out, n, 0);
     if (e != cudaSuccess) return from_cuda(e);
     return from_cuda(cudaDeviceSynchronize());

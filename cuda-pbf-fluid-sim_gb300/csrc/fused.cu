@@ -465,15 +465,13 @@ __device__ __forceinline__ void build_rows(const float4* __restrict__ pred, cons
 // derives its tile's plan itself.  The stencil's row ranges are reused while
 // consecutive particles share a cell.  A particle whose scene has no lists
 // gets the count cap + 1 (its warp walks the stencil).
-constexpr int kBuildBS = 256;
 template <class Scenes, class Sh>
-__global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restrict__ pred,
-                                                          const uint32_t* __restrict__ key_s,
-                                                          const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
-                                                          ListBufs lbuf, uint32_t* __restrict__ list,
-                                                          uint32_t* __restrict__ count, uint32_t* __restrict__ stats) {
+__device__ __forceinline__ void build_lists_warp(uint32_t s0, const float4* __restrict__ pred,
+                                                 const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                                 const Scenes& S, uint32_t N, const ListBufs& lbuf,
+                                                 uint32_t* __restrict__ list, uint32_t* __restrict__ count,
+                                                 uint32_t* __restrict__ stats) {
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t s0 = (blockIdx.x * kBuildBS + threadIdx.x) & ~31u;
     if (s0 >= N) return;  // warp-uniform
     const uint32_t cap = lbuf.cap;
     const WarpPlan plan = plan_tile_warp<Sh>(key_s, lb, S, lbuf, s0 - s0 % uint32_t(Sh::kTile), N);
@@ -648,6 +646,108 @@ __global__ void __launch_bounds__(kBuildBS) k_build_lists(const float4* __restri
     if (lane == 0 && stats) {
         atomicMax(stats, longest);
         if (overflowed) atomicAdd(stats + 1, overflowed);
+    }
+}
+
+// The list build of a whole tile (one CTA of Sh::kTile threads).  A staged
+// tile copies its stencil rows into shared memory, as the passes do, and
+// every thread builds its own particle's list from there: for each of its
+// rows it tests the row's cells (the slot range from the lower-bound table,
+// inside the tile's staged range) against its position, in walk order, and
+// emits the stage indices of the candidates within the list radius, eight
+// 16-bit entries to a 16-byte store.  That is a few instructions per
+// candidate instead of a warp step per 32 candidates of one particle.  The r^2
+// test is the passes' (dist2), so the lists are the same.  Tiles that are not
+// staged, or whose staging wait gave up, are built warp by warp from global
+// memory (build_lists_warp), which writes the same entries.
+template <class Scenes, class Sh>
+__global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* __restrict__ pred,
+                                                                 const uint32_t* __restrict__ key_s,
+                                                                 const uint32_t* __restrict__ lb, Scenes S,
+                                                                 uint32_t N, ListBufs lbuf,
+                                                                 uint32_t* __restrict__ list,
+                                                                 uint32_t* __restrict__ count,
+                                                                 uint32_t* __restrict__ stats,
+                                                                 uint32_t* __restrict__ err) {
+    extern __shared__ float4 smem[];
+    __shared__ TilePlan P;
+    __shared__ uint32_t s_longest, s_over;
+    float4* sp = smem;
+    const uint32_t t0 = blockIdx.x * Sh::kTile;
+    const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
+    if (!staged || !stageOk) {  // CTA-uniform
+        build_lists_warp<Scenes, Sh>(t0 + (threadIdx.x & ~31u), pred, key_s, lb, S, N, lbuf, list, count, stats);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        s_longest = 0;
+        s_over = 0;
+    }
+    __syncthreads();
+    const uint32_t s = t0 + threadIdx.x;
+    const uint32_t cap = lbuf.cap;
+    uint32_t cnt = 0;
+    if (s < N) {
+        const SceneView v = S.view(s);  // a staged tile lies in one scene, whose lists are on
+        const sim::DeviceParams& dp = *v.dp;
+        float R2 = 0.f;
+        list_radius2(dp, v.listUpdates, R2);
+        const uint32_t key = key_s[s];
+        const int reach = neighbour_reach(dp);
+        const int side = 2 * reach + 1;
+        const int nrows = side * side;  // <= kPlanRows in a staged tile
+        const int3 dim = dp.grid.dim;
+        int cx, cy, cz;
+        decode_key(key - v.cellOffset, dim, cx, cy, cz);
+        const int x0 = max(cx - reach, 0);
+        const int x1 = min(cx + reach, dim.x - 1);
+        const uint32_t* __restrict__ slb = lb + v.cellOffset;
+        const float4 pi = pred[s];
+        uint4* out = reinterpret_cast<uint4*>(list + size_t(s) * cap);  // 2 cap 16-bit entries of room
+        const uint32_t room = 2u * cap;
+        unsigned long long lo = 0ull, hi = 0ull;  // the chunk being filled: entries 0-3, 4-7
+        for (int r = 0; r < nrows; ++r) {
+            const int z = cz + r / side - reach;
+            const int y = cy + r % side - reach;
+            if (z < 0 || z >= dim.z || y < 0 || y >= dim.y) continue;
+            const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
+            // the row lies inside the tile's staged range for offset r; the
+            // clamp keeps every stage read in bounds regardless
+            const uint32_t b = max(__ldg(slb + row + uint32_t(x0)), P.start[r]);
+            const uint32_t e = min(__ldg(slb + row + uint32_t(x1) + 1u), P.start[r] + P.len[r]);
+            const uint32_t shift = P.base[r] - P.start[r];  // stage index of slot k: k + shift
+            for (uint32_t k = b; k < e; ++k) {
+                float rx, ry, rz;
+                if (k == s || dist2(pi, sp[k + shift], rx, ry, rz) > R2) continue;
+                const unsigned long long ent = (unsigned long long)((k + shift) & 0xFFFFu);
+                const uint32_t j = cnt & 7u;
+                if (j < 4u)
+                    lo |= ent << (16u * j);
+                else
+                    hi |= ent << (16u * (j - 4u));
+                ++cnt;
+                if (j == 7u) {
+                    if (cnt <= room) out[(cnt >> 3) - 1u] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi),
+                                                                       uint32_t(hi >> 32));
+                    lo = hi = 0ull;
+                }
+            }
+        }
+        if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room)
+            out[cnt >> 3] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi), uint32_t(hi >> 32));
+        count[s] = cnt;
+    }
+    const uint32_t longest = __reduce_max_sync(0xFFFFFFFFu, cnt);
+    const uint32_t over = __popc(__ballot_sync(0xFFFFFFFFu, cnt > cap));
+    if ((threadIdx.x & 31u) == 0) {
+        atomicMax(&s_longest, longest);
+        if (over) atomicAdd(&s_over, over);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && stats) {
+        atomicMax(stats, s_longest);
+        if (s_over) atomicAdd(stats + 1, s_over);
     }
 }
 
@@ -1066,10 +1166,12 @@ cudaError_t prepare_solve() {
 
 template <class Sh>
 cudaError_t prepare_shape() {
-    const int commit = int(Sh::kCommitSmem);
+    const int commit = int(Sh::kCommitSmem), stage = int(Sh::kStageBytes);
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
     if ((e = prepare_solve<Sh>()) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_build_lists_tiled<OneScene, Sh>, a, stage)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_build_lists_tiled<ManyScenes, Sh>, a, stage)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<OneScene, true, Sh>, a, commit)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<OneScene, false, Sh>, a, commit)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(k_commit<ManyScenes, true, Sh>, a, commit)) != cudaSuccess)
@@ -1113,11 +1215,14 @@ cudaError_t fused_prepare_kernels() {
 
 cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, cudaStream_t s) {
     if (sh.N == 0 || !lists_on(b, sh) || it < 0 || it >= sh.iters || it % sh.list_span != 0) return cudaErrorNotReady;
+    const cudaError_t pe = fused_prepare_kernels();
+    if (pe != cudaSuccess) return pe;
     const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
     return with_tile_shape(sh.tile, [&](auto shape) {
         using Sh = decltype(shape);
-        k_build_lists<OneScene, Sh><<<blocks_for(sh.N, kBuildBS), kBuildBS, 0, s>>>(
-            cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N, list_bufs(b, sh), b.nbr_list, b.nbr_count, b.nbr_stats);
+        k_build_lists_tiled<OneScene, Sh><<<blocks_for(sh.N, Sh::kTile), Sh::kTile, Sh::kStageBytes, s>>>(
+            cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N, list_bufs(b, sh), b.nbr_list, b.nbr_count, b.nbr_stats,
+            b.err);
         return cudaGetLastError();
     });
 }
@@ -1182,12 +1287,14 @@ cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t 
 // ------------------------------------------------------------ many scenes
 cudaError_t multi_build_lists(const MultiBufs& m, cudaStream_t s) {
     if (m.N == 0 || m.nbr_cap == 0) return cudaSuccess;
+    const cudaError_t pe = fused_prepare_kernels();
+    if (pe != cudaSuccess) return pe;
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
-        k_build_lists<ManyScenes, Sh><<<blocks_for(m.N, kBuildBS), kBuildBS, 0, s>>>(
+        k_build_lists_tiled<ManyScenes, Sh><<<blocks_for(m.N, Sh::kTile), Sh::kTile, Sh::kStageBytes, s>>>(
             m.pred_a, m.key_s, m.lb, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, lb, m.nbr_list, m.nbr_count,
-            m.nbr_stats);
+            m.nbr_stats, m.err);
         return cudaGetLastError();
     });
 }

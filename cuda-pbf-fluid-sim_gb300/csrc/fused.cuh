@@ -79,8 +79,8 @@ struct FusedShape {
     // Tile shape of the list passes (0 .. fused_tile_shape_count() - 1).
     int tile;
     // Arithmetic of the delta pass: false = exact (bit-identical to the
-    // reference kernels), true = fast (s_corr power without powf; within the
-    // 1e-5 bars).
+    // reference kernels), true = fast (s_corr power from error-free products
+    // instead of powf; within the 1e-5 bars).
     bool fast;
 };
 

@@ -243,6 +243,7 @@ __global__ void k_eval_math(int fn, const float* __restrict__ a, const float* __
         case 0: r = powf(a[i], b[i]); break;
         case 1: r = sqrtf(a[i]); break;
         case 2: r = a[i] / b[i]; break;
+        case 3: r = pow4_compensated(a[i]); break;
         default: r = 0.f; break;
     }
     out[i] = r;

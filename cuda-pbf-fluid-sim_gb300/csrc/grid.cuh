@@ -35,7 +35,8 @@ cudaError_t launch_compact(void* d_scratch, size_t scratch_bytes, uint32_t* uniq
                            uint32_t* count, uint32_t* seg, const uint32_t* keys_sorted, uint32_t N, cudaStream_t s,
                            uint32_t* err);
 
-// Device powf (fn 0), sqrtf (fn 1), division (fn 2) on arrays.
+// Device powf (fn 0), sqrtf (fn 1), division (fn 2) and the fast mode's
+// compensated x^4 (fn 3) on arrays.
 cudaError_t eval_math(int fn, const float* a, const float* b, float* out, uint32_t n, cudaStream_t s);
 
 // Exhaustive check of the s_corr exponent's n = 4 form (see

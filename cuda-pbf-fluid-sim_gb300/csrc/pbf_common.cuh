@@ -540,26 +540,29 @@ struct CompactRows {
 // ------------------------------------------------------- arithmetic modes
 // The delta pass comes in two modes (a template flag kFast).
 //   exact: the reference kernels' operations with explicit rounding, so
-//          results are bit-identical to the reference's FP32 kernels.
-//   fast:  the s_corr term without powf: ratio = w * (1 / w_q), with the
-//          reciprocal computed once per walk, and for n = 4 (the default)
-//          ratio^4 = (ratio^2)^2.  Everything else is the exact mode's.  The
-//          power is within ~1.5 ulp of the exact one (CUDA's powf itself is
-//          not correctly rounded), so per-step results stay within the 1e-5
-//          relative bars on state.  A mode that also replaced the correctly
-//          rounded square root and divisions of the spiky gradient by rsqrtf
-//          and reciprocals was measured and dropped: the last iteration's
-//          lambda then left its bar (1.8e-5 at 2 iterations, 1.0e-4 at 4).
-// Constants of the bodies, computed once per walk.
-struct NbrConsts {
-    float inv_wq;  // 1 / w_q, 0 when w_q <= 0 (fast mode)
-};
-
-template <bool kFast>
-__device__ __forceinline__ NbrConsts nbr_consts(float w_q) {
-    NbrConsts c;
-    c.inv_wq = (kFast && w_q > 0.f) ? __fdiv_rn(1.0f, w_q) : 0.f;
-    return c;
+//          results are bit-identical to the reference's FP32 kernels, whose
+//          s_corr power is CUDA's powf (about 65 instructions, and not
+//          correctly rounded: 6.3% of ratio^4 values are an ulp off).
+//   fast:  the s_corr power for n = 4 (the default) from error-free products
+//          (pow4_compensated, below): ratio^4 to within an ulp, in practice
+//          the correctly rounded value, in seven instructions.  Everything
+//          else is the exact mode's, so the step stays within the 1e-5
+//          relative bars on state; other exponents keep powf.  Two faster
+//          variants were measured and dropped: (ratio^2)^2 with a reciprocal
+//          of w_q (the last iteration's lambda at 1.05e-5 of the oracle's
+//          at 2 iterations), and rsqrtf / reciprocals for the spiky
+//          gradient as well (1.8e-5 at 2 iterations, 1.0e-4 at 4).
+// x^4 from error-free transformations: q + e = x^2 exactly (e = fma(x, x, -q)),
+// r + f = q^2 exactly, and x^4 = q^2 + 2 q e + e^2 = r + (f + 2 q e) with the
+// e^2 term below 2^-48 of the result.  The final sum rounds once, so the
+// result is within half an ulp of x^4 plus that tiny remainder: correctly
+// rounded except within ~2^-24 ulp of a rounding tie.  (x >= 0, as w / w_q is.)
+__device__ __forceinline__ float pow4_compensated(float x) {
+    const float q = __fmul_rn(x, x);
+    const float e = __fmaf_rn(x, x, -q);
+    const float r = __fmul_rn(q, q);
+    const float f = __fmaf_rn(q, q, -r);
+    return __fadd_rn(r, __fmaf_rn(__fmul_rn(2.0f, q), e, f));
 }
 
 // Spiky-gradient coefficient -3 spiky (h - r)^2 / max(r, grad_r_eps) of a
@@ -692,7 +695,7 @@ __device__ __forceinline__ float scorr_wq(const sim::DeviceParams& dp) {
 // One neighbour's term (l_ij, a_ij): the sum is d += l_ij * a_ij per axis.
 template <bool kFast = false>
 __device__ __forceinline__ float4 delta_term(float rx, float ry, float rz, float r2, float lam_i, float lam_j,
-                                             float w_q, const sim::DeviceParams& dp, const NbrConsts& c) {
+                                             float w_q, const sim::DeviceParams& dp) {
     const sim::KernelCoeffs& kc = dp.kernel;
     const sim::PbfTuning& pbf = dp.pbf;
     const float coeff = spiky_coeff(r2, dp);
@@ -701,19 +704,8 @@ __device__ __forceinline__ float4 delta_term(float rx, float ry, float rz, float
     if (pbf.scorr_enable) {
         const float hr2 = sub_(kc.h2, r2);
         const float w = mul_(mul_(mul_(kc.poly6, hr2), hr2), hr2);
-        float pw;
-        if (kFast) {
-            const float ratio = mul_(w, c.inv_wq);
-            if (pbf.scorr_n == 4.0f) {
-                const float q = mul_(ratio, ratio);
-                pw = mul_(q, q);
-            } else {
-                pw = powf(ratio, pbf.scorr_n);
-            }
-        } else {
-            const float ratio = (w_q > 0.f) ? div_(w, w_q) : 0.0f;
-            pw = scorr_pow(ratio, pbf.scorr_n);
-        }
+        const float ratio = (w_q > 0.f) ? div_(w, w_q) : 0.0f;
+        const float pw = (kFast && pbf.scorr_n == 4.0f) ? pow4_compensated(ratio) : scorr_pow(ratio, pbf.scorr_n);
         scorr = mul_(-pbf.scorr_k, pw);
         if (pbf.scorr_min < 0.f) scorr = fmaxf(scorr, pbf.scorr_min);
     }
@@ -728,9 +720,8 @@ __device__ __forceinline__ void delta_apply_term(float3& d, float4 term) {
 
 template <bool kFast = false>
 __device__ __forceinline__ void delta_accumulate(float3& d, float rx, float ry, float rz, float r2, float lam_i,
-                                                 float lam_j, float w_q, const sim::DeviceParams& dp,
-                                                 const NbrConsts& c) {
-    delta_apply_term(d, delta_term<kFast>(rx, ry, rz, r2, lam_i, lam_j, w_q, dp, c));
+                                                 float lam_j, float w_q, const sim::DeviceParams& dp) {
+    delta_apply_term(d, delta_term<kFast>(rx, ry, rz, r2, lam_i, lam_j, w_q, dp));
 }
 
 __device__ __forceinline__ float3 delta_finalize(float3 dsum, const sim::DeviceParams& dp) {
@@ -763,7 +754,6 @@ template <bool kFast = false, class RowRange, class Fetch>
 __device__ __forceinline__ float3 delta_of_sum(uint32_t self, float4 pi, float lam_i, int cx, int cy, int cz,
                                            const sim::DeviceParams& dp, float w_q, RowRange&& rows, Fetch&& fetch) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
-    const NbrConsts c = nbr_consts<kFast>(w_q);
     walk_neighbours(cx, cy, cz, neighbour_reach(dp), dp.grid.dim, rows, [&](uint32_t k) -> bool {
         uint32_t j;
         float lam_j;
@@ -772,7 +762,7 @@ __device__ __forceinline__ float3 delta_of_sum(uint32_t self, float4 pi, float l
         float rx, ry, rz;
         const float r2 = dist2(pi, pj, rx, ry, rz);
         if (r2 > dp.kernel.h2) return true;
-        delta_accumulate<kFast>(dsum, rx, ry, rz, r2, lam_i, lam_j, w_q, dp, c);
+        delta_accumulate<kFast>(dsum, rx, ry, rz, r2, lam_i, lam_j, w_q, dp);
         return true;
     });
     return dsum;
@@ -788,7 +778,6 @@ template <int Q, int kStride, bool kFast = false, class Src, class Data, class Q
 __device__ __forceinline__ float3 delta_queued_sum(bool active, uint32_t s, float4 pi, float lam_i, const Src& src,
                                                const sim::DeviceParams& dp, float w_q, const Data& data, QT* q) {
     float3 dsum = make_float3(0.f, 0.f, 0.f);
-    const NbrConsts c = nbr_consts<kFast>(w_q);
     const float h2 = dp.kernel.h2;
     constexpr bool kSelf = std::is_same<Src, RowSource>::value;
     walk_source<Q, kStride, false>(
@@ -801,7 +790,7 @@ __device__ __forceinline__ float3 delta_queued_sum(bool active, uint32_t s, floa
             float rx, ry, rz;
             const float4 pj = data.p(k);
             const float r2 = dist2(pi, pj, rx, ry, rz);
-            delta_accumulate<kFast>(dsum, rx, ry, rz, r2, lam_i, data.l(k, pj), w_q, dp, c);
+            delta_accumulate<kFast>(dsum, rx, ry, rz, r2, lam_i, data.l(k, pj), w_q, dp);
         });
     return dsum;
 }

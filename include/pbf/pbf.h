@@ -288,9 +288,10 @@ int pbf_autotune_tile_shape(pbf_sim* sim, const pbf_sim_params* p, int steps, fl
  * PBF_MATH_EXACT (the default) evaluates the reference kernels' operations
  * with their rounding: keys, permutation, cell tables, lambda, positions and
  * velocities are bit-identical to the reference's FP32 kernels.
- * PBF_MATH_FAST evaluates the s_corr term without powf: the ratio w / w_q as
- * a product with 1 / w_q, and for the default exponent n = 4 the power as
- * (ratio^2)^2.  Everything else is the exact mode's: keys, permutation,
+ * PBF_MATH_FAST computes the s_corr power for the default exponent n = 4
+ * from error-free products (ratio^4 correctly rounded except next to a
+ * rounding tie) instead of CUDA's powf, whose results are an ulp off for
+ * 6.3% of inputs.  Everything else is the exact mode's: keys, permutation,
  * cell tables and the first iteration's lambda stay bit-exact; lambda,
  * positions and velocities agree with the exact mode within 1e-5 relative
  * per step.  Takes effect at the next step. */
@@ -386,7 +387,8 @@ int pbf_density_grid(pbf_sim* sim, int res, float* d_grid);
 int pbf_density_grid_loss(pbf_sim* sim, int res, const float* d_target, double* loss, float4* d_pos_bar);
 
 /* Inspection: evaluates the device math the neighbour kernels use on
- * device arrays: fn 0 = powf(a, b), 1 = sqrtf(a), 2 = a / b (IEEE). */
+ * device arrays: fn 0 = powf(a, b), 1 = sqrtf(a), 2 = a / b (IEEE),
+ * 3 = a^4 as the fast arithmetic mode computes it (b unused). */
 int pbf_debug_eval_math(int fn, const float* d_a, const float* d_b, float* d_out, uint32_t n);
 
 /* The delta kernels evaluate s_corr's (w / w_q)^n with the exponent written

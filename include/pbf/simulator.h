@@ -136,8 +136,8 @@ public:
     bool setTileShape(int id);
     int tileShape() const { return m_bufs.tileShape; }
     // Arithmetic of the delta pass: 0 exact (the default; bit-identical to
-    // the reference kernels), 1 fast (the s_corr power as products instead of
-    // powf; per-step state within 1e-5 relative).  Takes effect at the next
+    // the reference kernels), 1 fast (the s_corr power from error-free
+    // products instead of powf; per-step state within 1e-5 relative).  Takes effect at the next
     // step (the step graph is captured again).
     bool setMathMode(int mode);
     int mathMode() const { return m_bufs.mathMode; }

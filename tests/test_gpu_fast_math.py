@@ -1,12 +1,13 @@
-"""PBF_MATH_FAST: the delta pass's s_corr term without powf (w / w_q as a
-product with the reciprocal, (ratio^2)^2 for the exponent n = 4).
+"""PBF_MATH_FAST: the delta pass's s_corr power for n = 4 from error-free
+products (ratio^4 correctly rounded except next to a tie) instead of CUDA's
+powf.
 
 Per step, from the same state, against the FP32 oracle: sorted keys,
 permutation and cell tables bit-exact (they come from the prediction, before
 any neighbour arithmetic), the first iteration's lambda bit-exact (the lambda
 pass is the exact mode's); the last iteration's lambda, positions and
 velocities within the bars of tests/parity.py (spec: 1e-5 relative on
-state).
+state).  The power itself is checked against a correctly rounded x^4.
 """
 import numpy as np
 import pytest
@@ -164,3 +165,35 @@ def test_fast_ensemble_against_oracle(gpu, lib, orc):
                 pbfx.oracle_step(orc, sc, True, opos, ovel, trace=False)
                 pbfx.assert_close(gpos[a:b], opos, STEP_POS, "scene %d positions" % si)
                 assert_velocities_close(gvel[a:b], ovel, opos, sc.dt)
+
+
+def test_compensated_pow4_is_correctly_rounded(gpu, lib):
+    """The fast mode's x^4 against x^4 rounded once from an exact value, on
+    2^22 random floats in [0, 2] plus powers of two and their neighbours:
+    equal wherever x^4 is not within 2^-20 ulp of a rounding tie."""
+    import ctypes as C
+
+    torch = gpu
+    rng = np.random.default_rng(4)
+    x = np.concatenate([rng.uniform(0.0, 2.0, 1 << 22).astype(np.float32),
+                        np.ldexp(np.float32(1.0), np.arange(-30, 30)).astype(np.float32),
+                        np.nextafter(np.ldexp(np.float32(1.0), np.arange(-30, 30)).astype(np.float32),
+                                     np.float32(np.inf)),
+                        np.float32([0.0, 1.0, 0.5, 0.25])])
+    a = torch.from_numpy(x).cuda()
+    out = torch.empty_like(a)
+    pbfx.check(lib.pbf_debug_eval_math(3, C.c_void_p(a.data_ptr()), C.c_void_p(a.data_ptr()),
+                                       C.c_void_p(out.data_ptr()), x.size), "eval_math")
+    got = out.cpu().numpy()
+    # x^2 is exact in float64 (48 significant bits); x^4 = (x^2)^2 rounded to
+    # float64 is within 2^-53 relative, so rounding it to float32 gives the
+    # correctly rounded x^4 unless x^4 lies that close to a float32 tie.
+    x64 = x.astype(np.float64)
+    q = x64 * x64
+    want64 = q * q
+    want = want64.astype(np.float32)
+    ulp = np.spacing(want).astype(np.float64)
+    frac = np.abs(want64 - want.astype(np.float64)) / np.where(ulp > 0, ulp, 1.0)
+    near_tie = np.abs(frac - 0.5) < 2.0 ** -20
+    bad = (got != want) & ~near_tie
+    assert not bad.any(), "x = %r: got %r, want %r" % (x[bad][:5], got[bad][:5], want[bad][:5])
