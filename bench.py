@@ -972,7 +972,7 @@ def run_ensemble(args, cfg, world, rank, local):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--autotune-steps", type=int, default=3,
                     help="steps per tile shape for the autotuner after warm-up (0: keep the default shape)")
