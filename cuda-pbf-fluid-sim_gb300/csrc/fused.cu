@@ -717,9 +717,7 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
             const uint32_t b = max(__ldg(slb + row + uint32_t(x0)), P.start[r]);
             const uint32_t e = min(__ldg(slb + row + uint32_t(x1) + 1u), P.start[r] + P.len[r]);
             const uint32_t shift = P.base[r] - P.start[r];  // stage index of slot k: k + shift
-            for (uint32_t k = b; k < e; ++k) {
-                float rx, ry, rz;
-                if (k == s || dist2(pi, sp[k + shift], rx, ry, rz) > R2) continue;
+            auto emit = [&](uint32_t k) {
                 const unsigned long long ent = (unsigned long long)((k + shift) & 0xFFFFu);
                 const uint32_t j = cnt & 7u;
                 if (j < 4u)
@@ -732,6 +730,21 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
                                                                        uint32_t(hi >> 32));
                     lo = hi = 0ull;
                 }
+            };
+            // two candidates per round: both loads and tests in flight, then
+            // the hits emitted in walk order
+            uint32_t k = b;
+            for (; k + 1u < e; k += 2u) {
+                float rx, ry, rz;
+                const float4 pa = sp[k + shift], pb = sp[k + 1u + shift];
+                const bool ha = k != s && !(dist2(pi, pa, rx, ry, rz) > R2);
+                const bool hb = k + 1u != s && !(dist2(pi, pb, rx, ry, rz) > R2);
+                if (ha) emit(k);
+                if (hb) emit(k + 1u);
+            }
+            if (k < e) {
+                float rx, ry, rz;
+                if (k != s && !(dist2(pi, sp[k + shift], rx, ry, rz) > R2)) emit(k);
             }
         }
         if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room)
