@@ -685,6 +685,7 @@ struct pbf_tape {
     uint32_t N = 0, numCells = 0;
     int steps = 0, every = 1, iters = 0, keyBits = 1;
     bool xsph = false;
+    bool fast = false;  // the forward's arithmetic mode: the replay uses the same delta pass
     cudaStream_t stream = nullptr;
     // replay engine (the fused step's buffers)
     float4 *pos = nullptr, *vel = nullptr;
@@ -729,6 +730,7 @@ struct pbf_tape {
         sh.hashed = false;
         sh.xsph = xsph;
         sh.list_span = listCap ? listSpan : 0;
+        sh.fast = fast;
         return sh;
     }
 
@@ -904,6 +906,7 @@ int pbf_forward(pbf_sim* h, int steps, int checkpoint_every, pbf_tape** out) {
     if (sp.pbf.xpbd_enable) return PBF_ERR_UNSUPPORTED;
     pbf_tape* t = nullptr;
     int st = make_tape(sp, N, steps, checkpoint_every, S.buffers().xsphEnabled && sp.xsph_c > 0.f, &t);
+    if (st == PBF_OK) t->fast = S.mathMode() == 1;
     if (st != PBF_OK) return st;
     const size_t b4 = sizeof(float4) * N;
     cudaStream_t s = S.cudaStream();

@@ -264,7 +264,8 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
     e->stream = e->own;
     if (ok) {  // neighbour lists: optional (without them every scene walks the stencil)
         const uint32_t cap = sim::Simulator::kDefaultListCapacity;
-        if (dalloc(&e->nbrList, size_t(N) * cap) && dalloc(&e->nbrCount, N)) {
+        // whole groups of 32 slots: staged tiles interleave the lists of a group
+        if (dalloc(&e->nbrList, size_t((uint64_t(N) + 31u) & ~uint64_t(31)) * cap) && dalloc(&e->nbrCount, N)) {
             e->nbrCap = cap;
         } else {
             cudaGetLastError();

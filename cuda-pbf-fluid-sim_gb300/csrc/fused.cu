@@ -367,10 +367,32 @@ __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigne
     return r;
 }
 
+// Layout of the lists.  Slot s owns cap 32-bit words of the list buffer.
+// Lists of tiles that are not staged hold sorted slots there, contiguously
+// (list + s * cap).  Lists of staged tiles hold 16-bit stage indices (2 cap of
+// room) and are interleaved by groups of 32 slots: the 32 lists of a group
+// share the group's 64 cap 16-bit entries, chunk c (entries 8c .. 8c + 7) of
+// slot s sitting at c * 256 + (s % 32) * 8.  A warp walking the same chunk of
+// its 32 lists then loads 512 contiguous bytes instead of 32 scattered 16-byte
+// pieces.  Tiles are whole groups, so a group holds one format; the buffer
+// holds a whole number of groups (allocations round the slots up to 32).
+constexpr uint32_t kListGroup = 32;
+constexpr uint32_t kList16ChunkStride = 8 * kListGroup;  // entries between a list's chunks
+__device__ __forceinline__ uint16_t* list16_base(uint32_t* list, uint32_t cap, uint32_t s) {
+    return reinterpret_cast<uint16_t*>(list) + size_t(s / kListGroup) * (2u * kListGroup * cap) +
+           (s % kListGroup) * 8u;
+}
+__device__ __forceinline__ const uint16_t* list16_base(const uint32_t* list, uint32_t cap, uint32_t s) {
+    return list16_base(const_cast<uint32_t*>(list), cap, s);
+}
+// Position of entry j of an interleaved 16-bit list.
+__device__ __forceinline__ uint32_t list16_at(uint32_t j) { return (j >> 3) * kList16ChunkStride + (j & 7u); }
+
 // One particle's list being written by a warp: hits of a 32-candidate step
-// are compacted with a ballot into consecutive entries (coalesced stores).
+// are compacted with a ballot into consecutive entries.
 struct ListWriter {
-    uint32_t* out;  // the particle's list (16-bit entries in staged tiles)
+    uint32_t* out;    // the particle's 32-bit list (tiles that are not staged)
+    uint16_t* out16;  // its interleaved 16-bit list (staged tiles)
     uint32_t cnt;
     __device__ __forceinline__ void emit(bool in, uint32_t k, uint32_t shift, uint32_t cap, bool staged,
                                          uint32_t lt) {
@@ -378,7 +400,7 @@ struct ListWriter {
         const uint32_t at = cnt + __popc(m & lt);
         if (in && at < cap) {
             if (staged)
-                reinterpret_cast<uint16_t*>(out)[at] = uint16_t(k + shift);
+                out16[list16_at(at)] = uint16_t(k + shift);
             else
                 out[at] = k;
         }
@@ -390,10 +412,14 @@ struct ListWriter {
     // then exceeds cap and the warp walks the stencil).
     __device__ __forceinline__ void emit16(bool in, uint32_t k, uint32_t shift, uint32_t cap, uint32_t lt) {
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, in);
-        if (in && cnt <= cap) reinterpret_cast<uint16_t*>(out)[cnt + __popc(m & lt)] = uint16_t(k + shift);
+        if (in && cnt <= cap) out16[list16_at(cnt + __popc(m & lt))] = uint16_t(k + shift);
         cnt += __popc(m);
     }
 };
+
+__device__ __forceinline__ ListWriter list_writer(uint32_t* list, uint32_t cap, uint32_t s) {
+    return ListWriter{list + size_t(s) * cap, list16_base(list, cap, s), 0u};
+}
 
 // One row of the list build for G particles of one cell: candidates [b, e),
 // 32 per step.  kSlack: staged tile with cap >= 32 (ListWriter::emit16).
@@ -553,7 +579,7 @@ __device__ __forceinline__ void build_lists_warp(uint32_t s0, const float4* __re
             for (int g = 0; g < 4; ++g) {
                 sl[g] = s + uint32_t(g);
                 pp[g] = pred[sl[g]];
-                w[g] = ListWriter{list + size_t(sl[g]) * cap, 0u};
+                w[g] = list_writer(list, cap, sl[g]);
             }
             if (slack)
                 build_rows<4, true>(pred, sl, pp, 4, nrows, rb, re, planShift, R2, cap, staged, lt, lane, w);
@@ -570,8 +596,8 @@ __device__ __forceinline__ void build_lists_warp(uint32_t s0, const float4* __re
         }
         const uint32_t sB = pair ? s + 1 : s;
         const float4 pa = pred[s], pb = pred[sB];
-        ListWriter wa{list + size_t(s) * cap, 0u};
-        ListWriter wb{list + size_t(sB) * cap, 0u};
+        ListWriter wa = list_writer(list, cap, s);
+        ListWriter wb = list_writer(list, cap, sB);
         if (flat) {
             for (uint32_t c = 0; c < T; c += 32u) {
                 const uint32_t vi = c + lane;
@@ -704,7 +730,8 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
         const int x1 = min(cx + reach, dim.x - 1);
         const uint32_t* __restrict__ slb = lb + v.cellOffset;
         const float4 pi = pred[s];
-        uint4* out = reinterpret_cast<uint4*>(list + size_t(s) * cap);  // 2 cap 16-bit entries of room
+        // the interleaved 16-bit list: chunk c at out[c * kListGroup] (2 cap entries of room)
+        uint4* out = reinterpret_cast<uint4*>(list16_base(list, cap, s));
         const uint32_t room = 2u * cap;
         unsigned long long lo = 0ull, hi = 0ull;  // the chunk being filled: entries 0-3, 4-7
         for (int r = 0; r < nrows; ++r) {
@@ -726,8 +753,9 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
                     hi |= ent << (16u * (j - 4u));
                 ++cnt;
                 if (j == 7u) {
-                    if (cnt <= room) out[(cnt >> 3) - 1u] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi),
-                                                                       uint32_t(hi >> 32));
+                    if (cnt <= room)
+                        out[size_t((cnt >> 3) - 1u) * kListGroup] =
+                            make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi), uint32_t(hi >> 32));
                     lo = hi = 0ull;
                 }
             };
@@ -748,7 +776,8 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
             }
         }
         if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room)
-            out[cnt >> 3] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi), uint32_t(hi >> 32));
+            out[size_t(cnt >> 3) * kListGroup] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi),
+                                                            uint32_t(hi >> 32));
         count[s] = cnt;
     }
     const uint32_t longest = __reduce_max_sync(0xFFFFFFFFu, cnt);
@@ -791,7 +820,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
-                                             ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                             ListSource<uint16_t>{list16_base(lbuf.list, lbuf.cap, sc), n, 0u, kList16ChunkStride}, dp,
                                              StagedData{sp, nullptr}, q16);
         else
             a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi, ListSource<uint32_t>{base, n, sc}, dp, g, q32);
@@ -849,7 +878,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i,
-                                            ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                            ListSource<uint16_t>{list16_base(lbuf.list, lbuf.cap, sc), n, 0u, kList16ChunkStride}, dp,
                                             w_q, StagedData{sp, nullptr}, q16);
         else
             d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i, ListSource<uint32_t>{base, n, sc}, dp, w_q, g,
@@ -937,7 +966,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
             const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
             if (staged)
                 vx = xsph_list_inline(xs, x, vv,
-                                      ListSource<uint16_t>{reinterpret_cast<const uint16_t*>(base), n, 0u}, dp,
+                                      ListSource<uint16_t>{list16_base(lbuf.list, lbuf.cap, sc), n, 0u, kList16ChunkStride}, dp,
                                       StagedData{sp, sv});
             else
                 vx = xsph_queued<kQueue, Sh::kTile>(xs, sc, x, vv, ListSource<uint32_t>{base, n, sc}, dp, g, q);

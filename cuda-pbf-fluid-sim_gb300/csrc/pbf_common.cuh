@@ -333,8 +333,9 @@ __device__ __forceinline__ void load8(const uint16_t* __restrict__ p, uint32_t (
 }
 
 // A particle's neighbour list: n entries in walk order (E = uint32_t: sorted
-// slots; E = uint16_t: indices into the tile staged in shared memory).  The
-// list is 16-byte aligned with at least round_up(n, 8) readable entries.
+// slots; E = uint16_t: indices into the tile staged in shared memory), read
+// in chunks of eight: chunk c at lst + c * chunkStride, 16-byte aligned, with
+// round_up(n, 8) readable entries.
 // `fill` is an index that is safe to read and is used by lanes past their
 // list's end (their results are discarded).
 template <class E>
@@ -342,6 +343,9 @@ struct ListSource {
     const E* __restrict__ lst;
     uint32_t n;
     uint32_t fill;
+    // entries from one chunk of eight to the next: 8 for a contiguous list,
+    // more for lists interleaved across the slots of a warp
+    uint32_t chunkStride = 8;
 };
 
 // Eight list entries held as loaded (one or two 16-byte words), unpacked on use.
@@ -419,7 +423,7 @@ __device__ __forceinline__ void walk_list_queued(bool active, const ListSource<E
             }
             e += kChunk;
             done = done || e >= n;
-            if (!done) cur.load(src.lst + e);
+            if (!done) cur.load(src.lst + size_t(e >> 3) * src.chunkStride);
         }
         const bool walking = __any_sync(0xFFFFFFFFu, !done);
         // lanes with nothing queued and nothing left to walk do not hold the
@@ -874,7 +878,7 @@ __device__ __forceinline__ float4 xsph_list_inline(bool active, float4 pi, float
     const uint32_t n = active ? src.n : 0u;
     for (uint32_t e = 0; e < n; e += 8) {
         uint32_t ks[8];
-        load8(src.lst + e, ks);
+        load8(src.lst + size_t(e >> 3) * src.chunkStride, ks);
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             if (e + uint32_t(u) < n) {

@@ -152,7 +152,8 @@ bool DeviceBuffers::allocateLists(uint32_t entries) {
     releaseLists();
     entries = (entries + 7u) & ~7u;
     if (entries == 0 || capacity == 0) return true;
-    const size_t n = size_t(capacity) * entries;
+    // whole groups of 32 slots: staged tiles interleave the lists of a group
+    const size_t n = size_t((capacity + 31u) & ~31u) * entries;
     if (!dalloc(&d_nbrList, n) || !dalloc(&d_nbrCount, capacity) || !dalloc(&d_nbrStats, 2)) {
         releaseLists();
         cudaGetLastError();
