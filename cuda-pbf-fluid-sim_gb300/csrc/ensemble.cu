@@ -97,9 +97,8 @@ struct pbf_ensemble {
     float4 *pos = nullptr, *vel = nullptr, *pred_a = nullptr, *pred_b = nullptr, *pos_s = nullptr, *vel_s = nullptr;
     float* lam = nullptr;
     uint32_t *keys = nullptr, *key_s = nullptr, *perm = nullptr, *lb = nullptr, *sceneOfId = nullptr,
-             *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr,
-             *nbrHList = nullptr, *nbrHCount = nullptr;
-    uint32_t nbrCap = 0, nbrHCap = 0;
+             *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr;
+    uint32_t nbrCap = 0;
     int tile = 0;  // tile shape of the list passes
     bool fast = false;  // arithmetic of the delta pass (PBF_MATH_FAST)
     pbf::SceneInfo* scenes = nullptr;
@@ -115,8 +114,7 @@ struct pbf_ensemble {
         if (graph) cudaGraphDestroy(graph);
         for (void* p : {(void*)pos, (void*)vel, (void*)pred_a, (void*)pred_b, (void*)pos_s, (void*)vel_s, (void*)lam,
                         (void*)keys, (void*)key_s, (void*)perm, (void*)lb, (void*)sceneOfId, (void*)sceneOfSlot,
-                        (void*)err, (void*)scenes, sortTemp, (void*)nbrList, (void*)nbrCount, (void*)nbrStats,
-                        (void*)nbrHList, (void*)nbrHCount})
+                        (void*)err, (void*)scenes, sortTemp, (void*)nbrList, (void*)nbrCount, (void*)nbrStats})
             if (p) cudaFree(p);
         if (own) cudaStreamDestroy(own);
     }
@@ -142,9 +140,6 @@ struct pbf_ensemble {
         m.nbr_count = nbrCount;
         m.nbr_stats = nbrStats;
         m.nbr_cap = nbrCap;
-        m.nbr_hlist = nbrHList;
-        m.nbr_hcount = nbrHCount;
-        m.nbr_hcap = nbrHCap;
         m.err = err;
         m.tile = tile;
         m.fast = fast;
@@ -270,18 +265,8 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
     if (ok) {  // neighbour lists: optional (without them every scene walks the stencil)
         const uint32_t cap = sim::Simulator::kDefaultListCapacity;
         // whole groups of 32 slots: staged tiles interleave the lists of a group
-        const size_t slots = size_t((uint64_t(N) + 31u) & ~uint64_t(31));
-        if (dalloc(&e->nbrList, slots * cap) && dalloc(&e->nbrCount, N)) {
+        if (dalloc(&e->nbrList, size_t((uint64_t(N) + 31u) & ~uint64_t(31)) * cap) && dalloc(&e->nbrCount, N)) {
             e->nbrCap = cap;
-            // within-h lists of the prediction: optional
-            if (dalloc(&e->nbrHList, slots * (cap / 2u)) && dalloc(&e->nbrHCount, N)) {
-                e->nbrHCap = cap / 2u;
-            } else {
-                cudaGetLastError();
-                if (e->nbrHList) cudaFree(e->nbrHList);
-                if (e->nbrHCount) cudaFree(e->nbrHCount);
-                e->nbrHList = e->nbrHCount = nullptr;
-            }
         } else {
             cudaGetLastError();
             if (e->nbrList) cudaFree(e->nbrList);

@@ -91,15 +91,6 @@ struct ListBufs {
     const uint32_t* __restrict__ count;
     uint32_t cap;  // 0: no lists
     int staging;   // 0: no tile is staged (all lists hold 32-bit slots)
-    // Neighbour lists of the build's own positions (staged tiles only): the
-    // list entries whose candidates lie within h at the positions the lists
-    // were built from, in walk order, as 16-bit stage indices interleaved like
-    // the lists; hcap 32-bit words (2 hcap entries) per slot, hcap 0: none.
-    // hcount[s] > 2 hcap: no such list for s (overflow, or a tile built from
-    // global memory).
-    const uint32_t* __restrict__ hlist = nullptr;
-    const uint32_t* __restrict__ hcount = nullptr;
-    uint32_t hcap = 0;
 };
 
 // Whether slot s's scene has lists this pass (the builder decided the same).
@@ -257,15 +248,6 @@ __device__ __forceinline__ bool warp_lists_fit(const ListBufs& lbuf, bool active
     return !__any_sync(0xFFFFFFFFu, n > lbuf.cap);
 }
 
-// Whether this warp walks its within-h lists (staged tiles, the build's
-// positions): every lane that walks has one that fits.  Every lane must call it.
-__device__ __forceinline__ bool warp_hits_fit(const ListBufs& lbuf, bool active, uint32_t sc, uint32_t& n) {
-    n = 0;
-    if (lbuf.hcap == 0) return false;
-    n = active ? lbuf.hcount[sc] : 0u;
-    return !__any_sync(0xFFFFFFFFu, n > 2u * lbuf.hcap);
-}
-
 __device__ __forceinline__ RowSource row_source(const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                 const SceneView& v, uint32_t sc) {
     RowSource r;
@@ -405,11 +387,6 @@ __device__ __forceinline__ const uint16_t* list16_base(const uint32_t* list, uin
 }
 // Position of entry j of an interleaved 16-bit list.
 __device__ __forceinline__ uint32_t list16_at(uint32_t j) { return (j >> 3) * kList16ChunkStride + (j & 7u); }
-
-// Slot sc's within-h list (ListBufs::hlist) of n entries.
-__device__ __forceinline__ ListSource<uint16_t> hits_source(const ListBufs& lbuf, uint32_t sc, uint32_t n) {
-    return ListSource<uint16_t>{list16_base(lbuf.hlist, lbuf.hcap, sc), n, 0u, kList16ChunkStride};
-}
 
 // One particle's list being written by a warp: hits of a 32-candidate step
 // are compacted with a ballot into consecutive entries.
@@ -698,36 +675,6 @@ __device__ __forceinline__ void build_lists_warp(uint32_t s0, const float4* __re
     }
 }
 
-// A thread's interleaved 16-bit list being written: entries gathered eight
-// to a 16-byte store at out[chunk * kListGroup]; room = entries that fit
-// (entries past it are counted, not stored).
-struct ChunkEmitter {
-    uint4* out;
-    uint32_t room;
-    uint32_t cnt = 0;
-    unsigned long long lo = 0ull, hi = 0ull;  // the chunk being filled: entries 0-3, 4-7
-    __device__ __forceinline__ void push(uint32_t stageIndex) {
-        const unsigned long long ent = (unsigned long long)(stageIndex & 0xFFFFu);
-        const uint32_t j = cnt & 7u;
-        if (j < 4u)
-            lo |= ent << (16u * j);
-        else
-            hi |= ent << (16u * (j - 4u));
-        ++cnt;
-        if (j == 7u) {
-            if (cnt <= room)
-                out[size_t((cnt >> 3) - 1u) * kListGroup] =
-                    make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi), uint32_t(hi >> 32));
-            lo = hi = 0ull;
-        }
-    }
-    __device__ __forceinline__ void flush() {
-        if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room)
-            out[size_t(cnt >> 3) * kListGroup] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi),
-                                                            uint32_t(hi >> 32));
-    }
-};
-
 // The list build of a whole tile (one CTA of Sh::kTile threads).  A staged
 // tile copies its stencil rows into shared memory, as the passes do, and
 // every thread builds its own particle's list from there: for each of its
@@ -747,9 +694,7 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
                                                                  uint32_t* __restrict__ list,
                                                                  uint32_t* __restrict__ count,
                                                                  uint32_t* __restrict__ stats,
-                                                                 uint32_t* __restrict__ err,
-                                                                 uint32_t* __restrict__ hlist,
-                                                                 uint32_t* __restrict__ hcount) {
+                                                                 uint32_t* __restrict__ err) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     __shared__ uint32_t s_longest, s_over;
@@ -757,9 +702,7 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
     const uint32_t t0 = blockIdx.x * Sh::kTile;
     const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
     const bool stageOk = stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
-    const uint32_t hcap = lbuf.hcap;
     if (!staged || !stageOk) {  // CTA-uniform
-        if (hcap && t0 + threadIdx.x < N) hcount[t0 + threadIdx.x] = 0xFFFFFFFFu;  // no within-h list
         build_lists_warp<Scenes, Sh>(t0 + (threadIdx.x & ~31u), pred, key_s, lb, S, N, lbuf, list, count, stats);
         return;
     }
@@ -787,10 +730,10 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
         const int x1 = min(cx + reach, dim.x - 1);
         const uint32_t* __restrict__ slb = lb + v.cellOffset;
         const float4 pi = pred[s];
-        const float h2 = dp.kernel.h2;
-        // the interleaved 16-bit lists: chunk c at out[c * kListGroup]
-        ChunkEmitter el{reinterpret_cast<uint4*>(list16_base(list, cap, s)), 2u * cap};
-        ChunkEmitter eh{hcap ? reinterpret_cast<uint4*>(list16_base(hlist, hcap, s)) : nullptr, 2u * hcap};
+        // the interleaved 16-bit list: chunk c at out[c * kListGroup] (2 cap entries of room)
+        uint4* out = reinterpret_cast<uint4*>(list16_base(list, cap, s));
+        const uint32_t room = 2u * cap;
+        unsigned long long lo = 0ull, hi = 0ull;  // the chunk being filled: entries 0-3, 4-7
         for (int r = 0; r < nrows; ++r) {
             const int z = cz + r / side - reach;
             const int y = cy + r % side - reach;
@@ -801,39 +744,41 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
             const uint32_t b = max(__ldg(slb + row + uint32_t(x0)), P.start[r]);
             const uint32_t e = min(__ldg(slb + row + uint32_t(x1) + 1u), P.start[r] + P.len[r]);
             const uint32_t shift = P.base[r] - P.start[r];  // stage index of slot k: k + shift
+            auto emit = [&](uint32_t k) {
+                const unsigned long long ent = (unsigned long long)((k + shift) & 0xFFFFu);
+                const uint32_t j = cnt & 7u;
+                if (j < 4u)
+                    lo |= ent << (16u * j);
+                else
+                    hi |= ent << (16u * (j - 4u));
+                ++cnt;
+                if (j == 7u) {
+                    if (cnt <= room)
+                        out[size_t((cnt >> 3) - 1u) * kListGroup] =
+                            make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi), uint32_t(hi >> 32));
+                    lo = hi = 0ull;
+                }
+            };
             // two candidates per round: both loads and tests in flight, then
-            // the hits emitted in walk order (within h: the passes' own test)
+            // the hits emitted in walk order
             uint32_t k = b;
             for (; k + 1u < e; k += 2u) {
                 float rx, ry, rz;
                 const float4 pa = sp[k + shift], pb = sp[k + 1u + shift];
-                const float ra = dist2(pi, pa, rx, ry, rz), rb = dist2(pi, pb, rx, ry, rz);
-                const bool ha = k != s && !(ra > R2);
-                const bool hb = k + 1u != s && !(rb > R2);
-                if (ha) {
-                    el.push(k + shift);
-                    if (hcap && !(ra > h2)) eh.push(k + shift);
-                }
-                if (hb) {
-                    el.push(k + 1u + shift);
-                    if (hcap && !(rb > h2)) eh.push(k + 1u + shift);
-                }
+                const bool ha = k != s && !(dist2(pi, pa, rx, ry, rz) > R2);
+                const bool hb = k + 1u != s && !(dist2(pi, pb, rx, ry, rz) > R2);
+                if (ha) emit(k);
+                if (hb) emit(k + 1u);
             }
             if (k < e) {
                 float rx, ry, rz;
-                const float ra = dist2(pi, sp[k + shift], rx, ry, rz);
-                if (k != s && !(ra > R2)) {
-                    el.push(k + shift);
-                    if (hcap && !(ra > h2)) eh.push(k + shift);
-                }
+                if (k != s && !(dist2(pi, sp[k + shift], rx, ry, rz) > R2)) emit(k);
             }
         }
-        el.flush();
-        count[s] = cnt = el.cnt;
-        if (hcap) {
-            eh.flush();
-            hcount[s] = eh.cnt;
-        }
+        if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room)
+            out[size_t(cnt >> 3) * kListGroup] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi),
+                                                            uint32_t(hi >> 32));
+        count[s] = cnt;
     }
     const uint32_t longest = __reduce_max_sync(0xFFFFFFFFu, cnt);
     const uint32_t over = __popc(__ballot_sync(0xFFFFFFFFu, cnt > cap));
@@ -853,8 +798,7 @@ template <class Scenes, class Sh>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf,
-                                                  uint32_t* __restrict__ err, float4* __restrict__ acc_out,
-                                                  int useHits) {
+                                                  uint32_t* __restrict__ err, float4* __restrict__ acc_out) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -872,9 +816,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     const bool stageOk = stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
     uint32_t n;
     LambdaAcc a;
-    if (useHits && staged && stageOk && warp_hits_fit(lbuf, active, sc, n)) {
-        a = lambda_hits_acc(active, pi, hits_source(lbuf, sc, n), dp, StagedData{sp, nullptr});
-    } else if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+    if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
@@ -912,7 +854,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
                                                  const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
                                                  float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
                                                  float4* __restrict__ vel_s, ListBufs lbuf,
-                                                 float4* __restrict__ dsum_out, int useHits) {
+                                                 float4* __restrict__ dsum_out) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -932,9 +874,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
     const GlobalData g{pred, lam, nullptr};
     uint32_t n;
     float3 d = make_float3(0.f, 0.f, 0.f);
-    if (useHits && staged && warp_hits_fit(lbuf, active, sc, n)) {
-        d = delta_hits_sum<kFast>(active, pi, lam_i, hits_source(lbuf, sc, n), dp, w_q, StagedData{sp, nullptr});
-    } else if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+    if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i,
@@ -1218,20 +1158,7 @@ int list_updates(const FusedShape& sh, int it) {
 
 ListBufs list_bufs(const FusedBufs& b, const FusedShape& sh) {
     if (!lists_on(b, sh)) return ListBufs{nullptr, nullptr, 0u, 0};
-    ListBufs l{b.nbr_list, b.nbr_count, b.nbr_cap, b.nbr_staging ? 1 : 0};
-    if (b.nbr_staging && b.nbr_hlist && b.nbr_hcount && b.nbr_hcap) {
-        l.hlist = b.nbr_hlist;
-        l.hcount = b.nbr_hcount;
-        l.hcap = b.nbr_hcap;
-    }
-    return l;
-}
-
-// The lambda / delta passes of iteration `it` read the positions the lists
-// were built from (and so may walk the within-h lists) when the lists were
-// built before this iteration's lambda.
-bool reads_build_positions(const FusedBufs& b, const FusedShape& sh, int it) {
-    return lists_on(b, sh) && b.nbr_hcap > 0 && it < sh.iters && it % sh.list_span == 0;
+    return ListBufs{b.nbr_list, b.nbr_count, b.nbr_cap, b.nbr_staging ? 1 : 0};
 }
 
 OneScene one_scene(const FusedBufs& b, const FusedShape& sh, int it) {
@@ -1335,10 +1262,9 @@ cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, 
     const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
     return with_tile_shape(sh.tile, [&](auto shape) {
         using Sh = decltype(shape);
-        const ListBufs lb = list_bufs(b, sh);
         k_build_lists_tiled<OneScene, Sh><<<blocks_for(sh.N, Sh::kTile), Sh::kTile, Sh::kStageBytes, s>>>(
-            cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N, lb, b.nbr_list, b.nbr_count, b.nbr_stats, b.err,
-            const_cast<uint32_t*>(lb.hlist), const_cast<uint32_t*>(lb.hcount));
+            cur, b.key_s, b.lb, one_scene(b, sh, it), sh.N, list_bufs(b, sh), b.nbr_list, b.nbr_count, b.nbr_stats,
+            b.err);
         return cudaGetLastError();
     });
 }
@@ -1356,14 +1282,12 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
         return with_math(sh.fast, [&](auto fast) {
             constexpr bool kFast = decltype(fast)::value;
             const unsigned g = blocks_for(sh.N, Sh::kTile);
-            const int hits = reads_build_positions(b, sh, it) ? 1 : 0;
             if (which == 0)
                 k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
-                    it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh), b.err, b.lambda_acc, hits);
+                    it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh), b.err, b.lambda_acc);
             else
                 k_delta<OneScene, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
-                    it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s, list_bufs(b, sh), b.delta_sum,
-                    hits);
+                    it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s, list_bufs(b, sh), b.delta_sum);
             return cudaGetLastError();
         });
     });
@@ -1403,28 +1327,16 @@ cudaError_t fused_commit(const FusedBufs& b, const FusedShape& sh, cudaStream_t 
 }
 
 // ------------------------------------------------------------ many scenes
-namespace {
-ListBufs multi_list_bufs(const MultiBufs& m) {
-    ListBufs l{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
-    if (m.nbr_hlist && m.nbr_hcount && m.nbr_hcap) {
-        l.hlist = m.nbr_hlist;
-        l.hcount = m.nbr_hcount;
-        l.hcap = m.nbr_hcap;
-    }
-    return l;
-}
-}  // namespace
-
 cudaError_t multi_build_lists(const MultiBufs& m, cudaStream_t s) {
     if (m.N == 0 || m.nbr_cap == 0) return cudaSuccess;
     const cudaError_t pe = fused_prepare_kernels();
     if (pe != cudaSuccess) return pe;
-    const ListBufs lb = multi_list_bufs(m);
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
         k_build_lists_tiled<ManyScenes, Sh><<<blocks_for(m.N, Sh::kTile), Sh::kTile, Sh::kStageBytes, s>>>(
             m.pred_a, m.key_s, m.lb, ManyScenes{m.scenes, m.sceneOfSlot}, m.N, lb, m.nbr_list, m.nbr_count,
-            m.nbr_stats, m.err, m.nbr_hlist, m.nbr_hcount);
+            m.nbr_stats, m.err);
         return cudaGetLastError();
     });
 }
@@ -1436,9 +1348,7 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
     float4* cur = (it % 2 == 0) ? m.pred_a : m.pred_b;
     float4* nxt = (it % 2 == 0) ? m.pred_b : m.pred_a;
     const ManyScenes sc{m.scenes, m.sceneOfSlot};
-    const ListBufs lb = multi_list_bufs(m);
-    // lists are built once per step, from the prediction iteration 0 reads
-    const int hits = (it == 0 && lb.hcap > 0) ? 1 : 0;
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
         return with_math(m.fast, [&](auto fast) {
@@ -1446,10 +1356,10 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
             const unsigned g = blocks_for(m.N, Sh::kTile);
             if (which == 0)
                 k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N,
-                                                                                    m.lam_s, lb, m.err, nullptr, hits);
+                                                                                    m.lam_s, lb, m.err, nullptr);
             else
                 k_delta<ManyScenes, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
-                    it, cur, m.lam_s, m.key_s, m.lb, sc, m.N, nxt, m.pos_s, m.vel_s, lb, nullptr, hits);
+                    it, cur, m.lam_s, m.key_s, m.lb, sc, m.N, nxt, m.pos_s, m.vel_s, lb, nullptr);
             return cudaGetLastError();
         });
     });
@@ -1459,7 +1369,7 @@ cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStrea
     if (m.N == 0) return cudaSuccess;
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
-    const ListBufs lb = multi_list_bufs(m);
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
         k_commit<ManyScenes, true, Sh><<<blocks_for(m.N, Sh::kTile), Sh::kTile, Sh::kCommitSmem, s>>>(

@@ -60,11 +60,6 @@ struct FusedBufs {
     uint32_t* nbr_count;
     uint32_t* nbr_stats;
     uint32_t nbr_cap;  // entries per particle, a multiple of 8; 0 = no lists
-    // Within-h lists of the build's positions (staged tiles): 16-bit entries,
-    // nbr_hcap 32-bit words per particle (0: none), counts in nbr_hcount.
-    uint32_t* nbr_hlist = nullptr;
-    uint32_t* nbr_hcount = nullptr;
-    uint32_t nbr_hcap = 0;
     // false: every list holds 32-bit sorted slots (no tile is staged), for
     // lists that are read outside the list passes (the adjoint)
     bool nbr_staging = true;
@@ -161,9 +156,6 @@ struct MultiBufs {
     const uint32_t *key_s, *perm, *lb;
     uint32_t *nbr_list, *nbr_count, *nbr_stats;
     uint32_t nbr_cap;  // 0: no lists
-    uint32_t* nbr_hlist = nullptr;  // within-h lists of the prediction (FusedBufs::nbr_hlist)
-    uint32_t* nbr_hcount = nullptr;
-    uint32_t nbr_hcap = 0;
     uint32_t* err;     // device error word (kErr* bits)
     int tile;          // tile shape of the list passes
     bool fast;         // arithmetic of the delta pass (FusedShape::fast)

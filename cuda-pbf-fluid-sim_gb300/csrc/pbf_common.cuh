@@ -678,39 +678,6 @@ __device__ __forceinline__ LambdaAcc lambda_queued_acc(bool active, uint32_t s, 
     return a;
 }
 
-// Walk of a list that holds exactly the particle's neighbours within h, in
-// walk order (built from the same positions): no distance test rejects an
-// entry and no queue is needed, so each lane runs its own entries' bodies.
-// The lambda cap keeps the first maxNeighbors of them, as the reference's walk
-// stops there.  Entries are read in chunks of eight (ListSource layout).
-template <class Data, class Body>
-__device__ __forceinline__ void walk_hits(bool active, const ListSource<uint16_t>& src, uint32_t limit,
-                                          const Data& data, Body&& body) {
-    const uint32_t n = active ? min(src.n, limit) : 0u;
-    ListChunk<uint16_t> ch;
-    for (uint32_t e = 0; e < n; e += 8u) {
-        ch.load(src.lst + size_t(e >> 3) * src.chunkStride);
-        const uint32_t m = min(8u, n - e);
-#pragma unroll
-        for (uint32_t u = 0; u < 8u; ++u)
-            if (u < m) body(ch.get(int(u)));
-    }
-}
-
-template <class Data>
-__device__ __forceinline__ LambdaAcc lambda_hits_acc(bool active, float4 pi, const ListSource<uint16_t>& src,
-                                                     const sim::DeviceParams& dp, const Data& data) {
-    LambdaAcc a;
-    const uint32_t limit = dp.maxNeighbors > 0 ? uint32_t(dp.maxNeighbors) : 0xFFFFFFFFu;
-    walk_hits(active, src, limit, data, [&](uint32_t k) {
-        float rx, ry, rz;
-        const float r2 = dist2(pi, data.p(k), rx, ry, rz);
-        lambda_accumulate(a, rx, ry, rz, r2, dp);
-        a.last = k;
-    });
-    return a;
-}
-
 // s_corr exponent: powf, as the reference (sim/pbf_delta_apply.cu:82).
 // With n = 4 exactly (the reference's default) the call names the exponent
 // at compile time, which the compiler evaluates with ~19 fewer instructions;
@@ -829,19 +796,6 @@ __device__ __forceinline__ float3 delta_queued_sum(bool active, uint32_t s, floa
             const float r2 = dist2(pi, pj, rx, ry, rz);
             delta_accumulate<kFast>(dsum, rx, ry, rz, r2, lam_i, data.l(k, pj), w_q, dp);
         });
-    return dsum;
-}
-
-template <bool kFast, class Data>
-__device__ __forceinline__ float3 delta_hits_sum(bool active, float4 pi, float lam_i, const ListSource<uint16_t>& src,
-                                                 const sim::DeviceParams& dp, float w_q, const Data& data) {
-    float3 dsum = make_float3(0.f, 0.f, 0.f);
-    walk_hits(active, src, 0xFFFFFFFFu, data, [&](uint32_t k) {
-        float rx, ry, rz;
-        const float4 pj = data.p(k);
-        const float r2 = dist2(pi, pj, rx, ry, rz);
-        delta_accumulate<kFast>(dsum, rx, ry, rz, r2, lam_i, data.l(k, pj), w_q, dp);
-    });
     return dsum;
 }
 

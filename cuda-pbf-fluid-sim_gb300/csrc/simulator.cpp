@@ -69,9 +69,6 @@ pbf::FusedBufs fused_bufs(DeviceBuffers& b, GridBuffers& g) {
     f.nbr_count = b.d_nbrCount;
     f.nbr_stats = b.d_nbrStats;
     f.nbr_cap = b.nbrListCap;
-    f.nbr_hlist = b.d_nbrHList;
-    f.nbr_hcount = b.d_nbrHCount;
-    f.nbr_hcap = b.nbrHListCap;
     return f;
 }
 
@@ -156,24 +153,14 @@ bool DeviceBuffers::allocateLists(uint32_t entries) {
     entries = (entries + 7u) & ~7u;
     if (entries == 0 || capacity == 0) return true;
     // whole groups of 32 slots: staged tiles interleave the lists of a group
-    const size_t slots = size_t((capacity + 31u) & ~31u);
-    const uint32_t hwords = entries / 2u;  // within-h lists: room for `entries` 16-bit entries
-    if (!dalloc(&d_nbrList, slots * entries) || !dalloc(&d_nbrCount, capacity) || !dalloc(&d_nbrStats, 2)) {
+    const size_t n = size_t((capacity + 31u) & ~31u) * entries;
+    if (!dalloc(&d_nbrList, n) || !dalloc(&d_nbrCount, capacity) || !dalloc(&d_nbrStats, 2)) {
         releaseLists();
         cudaGetLastError();
         return false;
     }
     cudaMemset(d_nbrStats, 0, 2 * sizeof(uint32_t));
     nbrListCap = entries;
-    // optional: without them the first iteration walks the lists as the others do
-    if (hwords >= 8u && dalloc(&d_nbrHList, slots * hwords) && dalloc(&d_nbrHCount, capacity)) {
-        nbrHListCap = hwords;
-    } else {
-        cudaGetLastError();
-        dfree(d_nbrHList);
-        dfree(d_nbrHCount);
-        nbrHListCap = 0;
-    }
     return true;
 }
 
@@ -181,10 +168,7 @@ void DeviceBuffers::releaseLists() {
     dfree(d_nbrList);
     dfree(d_nbrCount);
     dfree(d_nbrStats);
-    dfree(d_nbrHList);
-    dfree(d_nbrHCount);
     nbrListCap = 0;
-    nbrHListCap = 0;
 }
 
 void DeviceBuffers::release() {

@@ -52,12 +52,6 @@ struct DeviceBuffers {
     uint32_t* d_nbrCount = nullptr;
     uint32_t* d_nbrStats = nullptr;  // [0] longest list built, [1] overflowed lists
     uint32_t nbrListCap = 0;
-    // Within-h lists of the positions the lists are built from (staged tiles,
-    // 16-bit entries, nbrHListCap 32-bit words per particle): the first solver
-    // iteration walks them without distance tests.
-    uint32_t* d_nbrHList = nullptr;
-    uint32_t* d_nbrHCount = nullptr;
-    uint32_t nbrHListCap = 0;
     // Tile shape of the list passes (particles per CTA and staged slots; the
     // results do not depend on it).
     int tileShape = 0;
