@@ -733,7 +733,23 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
         // the interleaved 16-bit list: chunk c at out[c * kListGroup] (2 cap entries of room)
         uint4* out = reinterpret_cast<uint4*>(list16_base(list, cap, s));
         const uint32_t room = 2u * cap;
-        unsigned long long lo = 0ull, hi = 0ull;  // the chunk being filled: entries 0-3, 4-7
+        // The chunk being filled, as a shift register of eight 16-bit entries:
+        // each entry enters at the top of w3 and every earlier one moves down
+        // by 16 bits (funnel shifts), so after eight entries the first sits at
+        // the bottom of w0.  No branch on the entry's position in the chunk.
+        uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
+        uint32_t shift_of_row = 0;  // stage index of slot k in the current row: k + shift_of_row
+        auto shift_in = [&](uint32_t ent) {
+            w0 = __funnelshift_r(w0, w1, 16);
+            w1 = __funnelshift_r(w1, w2, 16);
+            w2 = __funnelshift_r(w2, w3, 16);
+            w3 = __funnelshift_r(w3, ent, 16);
+        };
+        auto emit = [&](uint32_t k) {
+            shift_in(k + shift_of_row);
+            ++cnt;
+            if ((cnt & 7u) == 0u && cnt <= room) out[size_t((cnt >> 3) - 1u) * kListGroup] = make_uint4(w0, w1, w2, w3);
+        };
         for (int r = 0; r < nrows; ++r) {
             const int z = cz + r / side - reach;
             const int y = cy + r % side - reach;
@@ -744,21 +760,7 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
             const uint32_t b = max(__ldg(slb + row + uint32_t(x0)), P.start[r]);
             const uint32_t e = min(__ldg(slb + row + uint32_t(x1) + 1u), P.start[r] + P.len[r]);
             const uint32_t shift = P.base[r] - P.start[r];  // stage index of slot k: k + shift
-            auto emit = [&](uint32_t k) {
-                const unsigned long long ent = (unsigned long long)((k + shift) & 0xFFFFu);
-                const uint32_t j = cnt & 7u;
-                if (j < 4u)
-                    lo |= ent << (16u * j);
-                else
-                    hi |= ent << (16u * (j - 4u));
-                ++cnt;
-                if (j == 7u) {
-                    if (cnt <= room)
-                        out[size_t((cnt >> 3) - 1u) * kListGroup] =
-                            make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi), uint32_t(hi >> 32));
-                    lo = hi = 0ull;
-                }
-            };
+            shift_of_row = shift;
             // two candidates per round: both loads and tests in flight, then
             // the hits emitted in walk order
             uint32_t k = b;
@@ -775,9 +777,11 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
                 if (k != s && !(dist2(pi, sp[k + shift], rx, ry, rz) > R2)) emit(k);
             }
         }
-        if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room)
-            out[size_t(cnt >> 3) * kListGroup] = make_uint4(uint32_t(lo), uint32_t(lo >> 32), uint32_t(hi),
-                                                            uint32_t(hi >> 32));
+        if ((cnt & 7u) && ((cnt + 7u) & ~7u) <= room) {
+            // the last, partial chunk: move its entries down to the bottom
+            for (uint32_t j = cnt & 7u; j < 8u; ++j) shift_in(0u);
+            out[size_t(cnt >> 3) * kListGroup] = make_uint4(w0, w1, w2, w3);
+        }
         count[s] = cnt;
     }
     const uint32_t longest = __reduce_max_sync(0xFFFFFFFFu, cnt);

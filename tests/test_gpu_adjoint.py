@@ -122,7 +122,9 @@ def test_velocity_gradient_matches_fp64_central_differences(gpu, lib, orc, probl
     loss, gv, _, _ = gpu_gradients(gpu, lib, p, pos, vel, target, steps, every=3)
     assert loss == pytest.approx(loss_f64(orc, p, pos, vel, target, steps), rel=1e-3)
     rng = np.random.default_rng(3)
-    coords = [(int(i), int(a)) for i, a in zip(rng.integers(0, pos.shape[0], 16), rng.integers(0, 3, 16))]
+    # 64 coordinates, as the benchmark spec's check asks: 56 random and the 8 the
+    # loss depends on most
+    coords = [(int(i), int(a)) for i, a in zip(rng.integers(0, pos.shape[0], 56), rng.integers(0, 3, 56))]
     # also the particles the loss depends on most
     top = np.argsort(-np.abs(gv[:, :3]).max(1))[:8]
     coords += [(int(i), int(np.argmax(np.abs(gv[i, :3])))) for i in top]
