@@ -720,48 +720,88 @@ def run_adjoint(args, cfg, world, rank, local):
     nx, ny, nz = cfg["lattice"]
     n = nx * ny * nz
     T, K, res = cfg["horizon"], cfg["every"], cfg["res"]
-    fwd_s = bwd_s = 0.0
-    losses, gnorm, cbar, finite = [], [], [], []
-    for sc in range(cfg["scenes"]):
-        p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
-        pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC5000 + sc, p)
-        rng = np.random.default_rng(0xC5000 + sc)
-        vstar = np.zeros_like(pos)
-        vstar[:, :3] = rng.uniform(-0.3, 0.3, (n, 3))
-        target = torch.zeros(res ** 3, dtype=torch.float32, device="cuda")
-        with pbfx.Sim(lib, p, hashed=cfg["hashed"]) as s:
+    S = cfg["scenes"]
+    sims, starts, targets = [], [], []
+    try:
+        for sc in range(S):
+            p = pbfx.dam_break_params(cfg["box"], cfg["iters"], n)
+            pos = pbfx.seed_lattice(lib, nx, ny, nz, (0.005, 0.005, 0.005), 0.01, 0.0005, 0xC5000 + sc, p)
+            rng = np.random.default_rng(0xC5000 + sc)
+            vstar = np.zeros_like(pos)
+            vstar[:, :3] = rng.uniform(-0.3, 0.3, (n, 3))
+            target = torch.zeros(res ** 3, dtype=torch.float32, device="cuda")
+            s = pbfx.Sim(lib, p, hashed=cfg["hashed"])
+            sims.append(s)
             s.upload(pos, vstar)  # target: the density after a run from seeded velocities
             s.step(T)
             pbfx.check(lib.pbf_density_grid(s.h, res, C.c_void_p(target.data_ptr())))
-            v0 = np.zeros_like(pos)
-            s.upload(pos, v0)
+            s.upload(pos, np.zeros_like(pos))
             s.step(1)  # graph capture outside the timing
-            s.upload(pos, v0)
+            starts.append(pos)
+            targets.append(target)
+
+        def adjoint_run(batched, pbar=None):
+            """Forward T steps and backward of the 32 scenes from their seeded
+            lattices at rest; (forward s, backward s, losses, dL/dv0, dL/dc,
+            final positions, dL/dx_T).  pbar: dL/dx_T to use instead of the
+            loss's (which scatters with float atomics, so its bits vary run
+            to run)."""
+            for s, pos in zip(sims, starts):
+                s.upload(pos, np.zeros_like(pos))
             torch.cuda.synchronize()
-            tape = C.c_void_p()
             t0 = time.perf_counter()
-            pbfx.check(lib.pbf_forward(s.h, T, K, C.byref(tape)))
+            if batched:
+                tapes = pbfx.forward_batch(lib, sims, T, K)
+            else:
+                tapes = []
+                for s in sims:
+                    t = C.c_void_p()
+                    pbfx.check(lib.pbf_forward(s.h, T, K, C.byref(t)))
+                    tapes.append(t)
             torch.cuda.synchronize()
-            fwd_s += time.perf_counter() - t0
+            fwd = time.perf_counter() - t0
             try:
-                pbar = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
-                vbar = torch.zeros_like(pbar)
-                g0 = torch.zeros_like(pbar)
-                loss, cb = C.c_double(), C.c_float()
-                pbfx.check(lib.pbf_density_grid_loss(s.h, res, C.c_void_p(target.data_ptr()), C.byref(loss),
-                                                     C.c_void_p(pbar.data_ptr())))
+                finals = [s.download()[0] for s in sims]
+                fresh = pbar is None
+                if fresh:
+                    pbar = [torch.zeros((n, 4), dtype=torch.float32, device="cuda") for _ in range(S)]
+                vbar = [torch.zeros_like(x) for x in pbar]
+                g0 = [torch.zeros_like(x) for x in pbar]
+                losses = []
+                for s, tg, pb in zip(sims, targets, pbar):
+                    loss = C.c_double()
+                    pbfx.check(lib.pbf_density_grid_loss(s.h, res, C.c_void_p(tg.data_ptr()), C.byref(loss),
+                                                         C.c_void_p(pb.data_ptr()) if fresh else None))
+                    losses.append(loss.value)
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
-                pbfx.check(lib.pbf_backward(tape, C.c_void_p(pbar.data_ptr()), C.c_void_p(vbar.data_ptr()), None,
-                                            C.c_void_p(g0.data_ptr()), C.byref(cb)))
+                if batched:
+                    cb = pbfx.backward_batch(lib, tapes, [x.data_ptr() for x in pbar], [x.data_ptr() for x in vbar],
+                                             None, [x.data_ptr() for x in g0])
+                else:
+                    cb = []
+                    for t, pb, vb, g in zip(tapes, pbar, vbar, g0):
+                        c = C.c_float()
+                        pbfx.check(lib.pbf_backward(t, C.c_void_p(pb.data_ptr()), C.c_void_p(vb.data_ptr()), None,
+                                                    C.c_void_p(g.data_ptr()), C.byref(c)))
+                        cb.append(c.value)
                 torch.cuda.synchronize()
-                bwd_s += time.perf_counter() - t0
-                losses.append(loss.value)
-                gnorm.append(float(torch.linalg.norm(g0[:, :3]).item()))
-                cbar.append(cb.value)
-                finite.append(float(torch.isfinite(g0[:, :3]).float().mean().item()))
+                bwd = time.perf_counter() - t0
+                return fwd, bwd, losses, [x[:, :3].cpu().numpy() for x in g0], cb, finals, pbar
             finally:
-                lib.pbf_tape_destroy(tape)
+                for t in tapes:
+                    lib.pbf_tape_destroy(t)
+
+        fwd_s, bwd_s, losses, grads, cbar, finals, pbar = adjoint_run(True)
+        sfwd_s, sbwd_s, _, sgrads, scbar, sfinals, _ = adjoint_run(False, pbar)
+    finally:
+        for s in sims:
+            s.close()
+    same_state = all(np.array_equal(a, b) for a, b in zip(finals, sfinals))
+    same_bits = all(np.array_equal(a, b, equal_nan=True) for a, b in zip(grads, sgrads)) and all(
+        a == b or (a != a and b != b) for a, b in zip(cbar, scbar))
+    gnorm = [float(np.linalg.norm(g)) for g in grads]
+    finite = [float(np.isfinite(g).mean()) for g in grads]
     # Gradient norm against the horizon, first scene: the reference's default
     # constants make the step chaotic (FP32 and FP64 runs separate ~10x per
     # step), so |dL/dv0| grows geometrically with the horizon.
@@ -797,7 +837,6 @@ def run_adjoint(args, cfg, world, rank, local):
                 ratio_by_h[str(H)] = tb / tf
             finally:
                 lib.pbf_tape_destroy(tape)
-    S = cfg["scenes"]
     ratio = bwd_s / fwd_s
     line = {
         "metric": "adjoint/fwd time", "value": ratio, "unit": "backward time / forward time", "n_gpus": world,
@@ -806,8 +845,17 @@ def run_adjoint(args, cfg, world, rank, local):
         "config": {"workload": cfg["workload"], "scenes": S, "particles_per_scene": n, "solver_iters": cfg["iters"],
                    "checkpoint_every": K, "grid_points": res ** 3, "parallelism": "single"},
         "forward_ms_per_step": 1e3 * fwd_s / (S * T), "backward_ms_per_step": 1e3 * bwd_s / (S * T),
+        "timed": "the 32 scenes as one batch: pbf_forward_batch (each scene's steps on its own stream, one "
+                 "synchronisation) and pbf_backward_batch; per step = per scene-step of the batch",
         "backward_includes": "the replay of each checkpoint segment (one recorded forward step per step) and the "
                              "adjoint kernels",
+        "scene_by_scene": {"value": sbwd_s / sfwd_s, "forward_ms_per_step": 1e3 * sfwd_s / (S * T),
+                           "backward_ms_per_step": 1e3 * sbwd_s / (S * T),
+                           "batch_speedup": (sfwd_s + sbwd_s) / (fwd_s + bwd_s),
+                           "final_states_identical_to_batch": bool(same_state),
+                           "gradients_identical_to_batch": bool(same_bits),
+                           "what": "the same 32 scenes through pbf_forward / pbf_backward one scene at a time "
+                                   "(each call synchronises), from the same states and with the batch's dL/dx_T"},
         "loss_mean": float(np.mean(losses)), "grad_v0_norm_mean": float(np.mean(gnorm)),
         "grad_xsph_c_mean": float(np.mean(cbar)),
         "grad_v0_norm_by_horizon": growth,
@@ -820,7 +868,7 @@ def run_adjoint(args, cfg, world, rank, local):
                          "finite (1-16 steps).  Per-step vector-Jacobian products are checked against an FP64 tape "
                          "in tests/test_gpu_adjoint_vjp.py",
         "e2e": {"value": ratio, "unit": "backward time / forward time", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0, "note": "host wall clock around pbf_forward / pbf_backward"},
+                "d2h_bytes_per_step": 0, "note": "host wall clock around pbf_forward_batch / pbf_backward_batch"},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

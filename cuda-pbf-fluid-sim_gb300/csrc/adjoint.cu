@@ -892,74 +892,146 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
     return PBF_OK;
 }
 
+// The parts of pbf_forward / pbf_backward that a batch interleaves across its
+// scenes: everything is enqueued on the scene's stream (the handle's for the
+// forward, the tape's own for the backward), and nothing waits until the
+// caller synchronises every stream of the batch.
+int tape_for(pbf_sim* h, int steps, int every, pbf_tape** out) {
+    sim::Simulator& S = h->sim;
+    const sim::SimParams& sp = S.params();
+    if (sp.pbf.xpbd_enable) return PBF_ERR_UNSUPPORTED;
+    const int st = make_tape(sp, S.activeParticleCount(), steps, every, S.buffers().xsphEnabled && sp.xsph_c > 0.f,
+                             out);
+    if (st == PBF_OK) (*out)->fast = S.mathMode() == 1;
+    return st;
+}
+
+// Step n of the forward: the checkpoint when n starts a segment, then the step.
+bool forward_step(pbf_sim* h, pbf_tape* t, int n) {
+    sim::Simulator& S = h->sim;
+    if (n % t->every == 0) {
+        const int c = n / t->every;
+        const size_t b4 = sizeof(float4) * t->N;
+        cudaStream_t s = S.cudaStream();
+        if (cudaMemcpyAsync(t->ckPos[c], S.devicePositions(), b4, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(t->ckVel[c], S.deviceVel(), b4, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return false;
+    }
+    return S.step(t->p);
+}
+
+cudaError_t backward_begin(pbf_tape* t, const float4* d_pos_bar, const float4* d_vel_bar) {
+    const size_t b4 = sizeof(float4) * t->N;
+    cudaMemcpyAsync(t->pbar, d_pos_bar, b4, cudaMemcpyDeviceToDevice, t->stream);
+    cudaMemcpyAsync(t->vbar, d_vel_bar, b4, cudaMemcpyDeviceToDevice, t->stream);
+    return cudaMemsetAsync(t->cbar, 0, sizeof(float), t->stream);
+}
+
+cudaError_t backward_load(pbf_tape* t, int c) {
+    const size_t b4 = sizeof(float4) * t->N;
+    cudaMemcpyAsync(t->pos, t->ckPos[c], b4, cudaMemcpyDeviceToDevice, t->stream);
+    return cudaMemcpyAsync(t->vel, t->ckVel[c], b4, cudaMemcpyDeviceToDevice, t->stream);
+}
+
+cudaError_t backward_end(pbf_tape* t, float4* d_pos0_bar, float4* d_vel0_bar) {
+    const size_t b4 = sizeof(float4) * t->N;
+    if (d_pos0_bar) cudaMemcpyAsync(d_pos0_bar, t->pbar, b4, cudaMemcpyDeviceToDevice, t->stream);
+    if (d_vel0_bar) cudaMemcpyAsync(d_vel0_bar, t->vbar, b4, cudaMemcpyDeviceToDevice, t->stream);
+    return cudaGetLastError();
+}
+
+// After the tape's stream has drained: the kernels' error word and dL/dc.
+int backward_result(pbf_tape* t, float* xsph_c_bar) {
+    uint32_t err = 0;
+    float cb = 0.f;
+    if (cudaMemcpy(&err, t->err, sizeof(err), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(&cb, t->cbar, sizeof(cb), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return PBF_ERR_CUDA;
+    if (err) return (err & pbf::kErrTimeoutBits) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
+    if (xsph_c_bar) *xsph_c_bar = cb;
+    return PBF_OK;
+}
+
+template <class T>
+bool distinct(const T* const* v, int count) {
+    for (int i = 0; i < count; ++i)
+        for (int j = 0; j < i; ++j)
+            if (v[i] == v[j]) return false;
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
 
+int pbf_forward_batch(pbf_sim* const* sims, int count, int steps, int checkpoint_every, pbf_tape** tapes) {
+    if (!tapes || count <= 0) return PBF_ERR_INVALID;
+    for (int i = 0; i < count; ++i) tapes[i] = nullptr;
+    if (!sims || steps <= 0 || checkpoint_every <= 0) return PBF_ERR_INVALID;
+    for (int i = 0; i < count; ++i)
+        if (!sims[i]) return PBF_ERR_INVALID;
+    if (!distinct(sims, count)) return PBF_ERR_INVALID;
+    int st = PBF_OK;
+    for (int i = 0; i < count && st == PBF_OK; ++i) st = tape_for(sims[i], steps, checkpoint_every, &tapes[i]);
+    // Step n of every scene before step n + 1 of any: the scenes' streams
+    // run side by side.
+    for (int n = 0; n < steps && st == PBF_OK; ++n)
+        for (int i = 0; i < count && st == PBF_OK; ++i)
+            if (!forward_step(sims[i], tapes[i], n)) st = PBF_ERR_CUDA;
+    for (int i = 0; i < count; ++i) {
+        const cudaError_t e = cudaStreamSynchronize(sims[i]->sim.cudaStream());
+        if (st == PBF_OK && e != cudaSuccess) st = pbf::status_of(e);
+    }
+    if (st != PBF_OK)
+        for (int i = 0; i < count; ++i) {
+            delete tapes[i];
+            tapes[i] = nullptr;
+        }
+    return st;
+}
+
 int pbf_forward(pbf_sim* h, int steps, int checkpoint_every, pbf_tape** out) {
     if (!out) return PBF_ERR_INVALID;
     *out = nullptr;
-    if (!h || steps <= 0 || checkpoint_every <= 0) return PBF_ERR_INVALID;
-    sim::Simulator& S = h->sim;
-    const sim::SimParams& sp = S.params();
-    const uint32_t N = S.activeParticleCount();
-    if (sp.pbf.xpbd_enable) return PBF_ERR_UNSUPPORTED;
-    pbf_tape* t = nullptr;
-    int st = make_tape(sp, N, steps, checkpoint_every, S.buffers().xsphEnabled && sp.xsph_c > 0.f, &t);
-    if (st == PBF_OK) t->fast = S.mathMode() == 1;
-    if (st != PBF_OK) return st;
-    const size_t b4 = sizeof(float4) * N;
-    cudaStream_t s = S.cudaStream();
-    for (int n = 0; n < steps; ++n) {
-        if (n % checkpoint_every == 0) {
-            const int c = n / checkpoint_every;
-            cudaMemcpyAsync(t->ckPos[c], S.devicePositions(), b4, cudaMemcpyDeviceToDevice, s);
-            cudaMemcpyAsync(t->ckVel[c], S.deviceVel(), b4, cudaMemcpyDeviceToDevice, s);
-        }
-        if (!S.step(sp)) {
-            delete t;
-            return PBF_ERR_CUDA;
-        }
+    if (!h) return PBF_ERR_INVALID;
+    return pbf_forward_batch(&h, 1, steps, checkpoint_every, out);
+}
+
+int pbf_backward_batch(pbf_tape* const* tapes, int count, const float4* const* d_pos_bar,
+                       const float4* const* d_vel_bar, float4* const* d_pos0_bar, float4* const* d_vel0_bar,
+                       float* xsph_c_bar) {
+    if (!tapes || count <= 0 || !d_pos_bar || !d_vel_bar) return PBF_ERR_INVALID;
+    for (int i = 0; i < count; ++i)
+        if (!tapes[i] || !d_pos_bar[i] || !d_vel_bar[i] || tapes[i]->steps != tapes[0]->steps ||
+            tapes[i]->every != tapes[0]->every)
+            return PBF_ERR_INVALID;
+    if (!distinct(tapes, count)) return PBF_ERR_INVALID;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < count && e == cudaSuccess; ++i) e = backward_begin(tapes[i], d_pos_bar[i], d_vel_bar[i]);
+    const pbf_tape& t0 = *tapes[0];
+    for (int c = int(t0.ckPos.size()) - 1; c >= 0 && e == cudaSuccess; --c) {
+        const int len = std::min(t0.every, t0.steps - c * t0.every);
+        for (int i = 0; i < count && e == cudaSuccess; ++i) e = backward_load(tapes[i], c);
+        for (int n = 0; n < len && e == cudaSuccess; ++n)
+            for (int i = 0; i < count && e == cudaSuccess; ++i) e = tapes[i]->record_step(tapes[i]->rec[n]);
+        for (int n = len - 1; n >= 0 && e == cudaSuccess; --n)
+            for (int i = 0; i < count && e == cudaSuccess; ++i) e = tapes[i]->adjoint_step(tapes[i]->rec[n]);
     }
-    const cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        delete t;
-        return pbf::status_of(e);
+    for (int i = 0; i < count && e == cudaSuccess; ++i)
+        e = backward_end(tapes[i], d_pos0_bar ? d_pos0_bar[i] : nullptr, d_vel0_bar ? d_vel0_bar[i] : nullptr);
+    int st = pbf::status_of(e);
+    for (int i = 0; i < count; ++i) {
+        const cudaError_t se = cudaStreamSynchronize(tapes[i]->stream);
+        if (st == PBF_OK && se != cudaSuccess) st = pbf::status_of(se);
     }
-    *out = t;
-    return PBF_OK;
+    for (int i = 0; i < count && st == PBF_OK; ++i) st = backward_result(tapes[i], xsph_c_bar ? xsph_c_bar + i : nullptr);
+    return st;
 }
 
 int pbf_backward(pbf_tape* t, const float4* d_pos_bar, const float4* d_vel_bar, float4* d_pos0_bar,
                  float4* d_vel0_bar, float* xsph_c_bar) {
     if (!t || !d_pos_bar || !d_vel_bar) return PBF_ERR_INVALID;
-    const size_t b4 = sizeof(float4) * t->N;
-    cudaStream_t s = t->stream;
-    cudaMemcpyAsync(t->pbar, d_pos_bar, b4, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(t->vbar, d_vel_bar, b4, cudaMemcpyDeviceToDevice, s);
-    cudaMemsetAsync(t->cbar, 0, sizeof(float), s);
-    const int segs = int(t->ckPos.size());
-    for (int c = segs - 1; c >= 0; --c) {
-        const int start = c * t->every;
-        const int len = std::min(t->every, t->steps - start);
-        cudaMemcpyAsync(t->pos, t->ckPos[c], b4, cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(t->vel, t->ckVel[c], b4, cudaMemcpyDeviceToDevice, s);
-        for (int n = 0; n < len; ++n)
-            if (t->record_step(t->rec[n]) != cudaSuccess) return PBF_ERR_CUDA;
-        for (int n = len - 1; n >= 0; --n)
-            if (t->adjoint_step(t->rec[n]) != cudaSuccess) return PBF_ERR_CUDA;
-    }
-    if (d_pos0_bar) cudaMemcpyAsync(d_pos0_bar, t->pbar, b4, cudaMemcpyDeviceToDevice, s);
-    if (d_vel0_bar) cudaMemcpyAsync(d_vel0_bar, t->vbar, b4, cudaMemcpyDeviceToDevice, s);
-    float cb = 0.f;
-    cudaMemcpyAsync(&cb, t->cbar, sizeof(float), cudaMemcpyDeviceToHost, s);
-    const cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return pbf::status_of(e);
-    uint32_t err = 0;
-    cudaMemcpy(&err, t->err, sizeof(err), cudaMemcpyDeviceToHost);
-    if (err) return (err & pbf::kErrTimeoutBits) ? PBF_ERR_TIMEOUT : PBF_ERR_CUDA;
-    if (xsph_c_bar) *xsph_c_bar = cb;
-    return PBF_OK;
+    return pbf_backward_batch(&t, 1, &d_pos_bar, &d_vel_bar, &d_pos0_bar, &d_vel0_bar, xsph_c_bar);
 }
 
 int pbf_tape_destroy(pbf_tape* t) {

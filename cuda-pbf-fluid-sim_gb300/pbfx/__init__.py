@@ -159,6 +159,8 @@ _SIGS = {
     "pbf_forward": ([_VP, _I, _I, C.POINTER(_VP)], _I),
     "pbf_backward": ([_VP, _VP, _VP, _VP, _VP, C.POINTER(_F)], _I),
     "pbf_tape_destroy": ([_VP], _I),
+    "pbf_forward_batch": ([_VP, _I, _I, _I, _VP], _I),
+    "pbf_backward_batch": ([_VP, _I, _VP, _VP, _VP, _VP, _VP], _I),
     "pbf_density_grid": ([_VP, _I, _VP], _I),
     "pbf_density_grid_loss": ([_VP, _I, _VP, C.POINTER(C.c_double), _VP], _I),
     "pbf_ensemble_create": ([C.POINTER(SimParams), _U32, C.POINTER(_VP)], _I),
@@ -452,6 +454,28 @@ class Sim:
         out = (C.c_double * 4)()
         check(self.lib.pbf_density_stats(self.h, C.byref(out)), "density_stats")
         return list(out)
+
+
+def forward_batch(lib, sims, steps: int, every: int):
+    """pbf_forward_batch over Sim objects; returns their tapes (c_void_p)."""
+    k = len(sims)
+    tapes = (_VP * k)()
+    check(lib.pbf_forward_batch((_VP * k)(*[s.h.value for s in sims]), k, steps, every, tapes), "forward_batch")
+    return [C.c_void_p(t) for t in tapes]
+
+
+def backward_batch(lib, tapes, pos_bar, vel_bar, pos0_bar=None, vel0_bar=None):
+    """pbf_backward_batch; the *_bar arguments are lists of device pointers
+    (ints), one per scene; returns dL/d(xsph_c) of each scene."""
+    k = len(tapes)
+
+    def arr(v):
+        return None if v is None else (_VP * k)(*v)
+
+    cb = (_F * k)()
+    check(lib.pbf_backward_batch((_VP * k)(*[t.value for t in tapes]), k, arr(pos_bar), arr(vel_bar), arr(pos0_bar),
+                                 arr(vel0_bar), cb), "backward_batch")
+    return [float(x) for x in cb]
 
 
 class Ensemble:

@@ -378,8 +378,24 @@ int pbf_forward(pbf_sim* sim, int steps, int checkpoint_every, pbf_tape** tape);
 int pbf_backward(pbf_tape* tape, const float4* d_pos_bar, const float4* d_vel_bar, float4* d_pos0_bar,
                  float4* d_vel0_bar, float* xsph_c_bar);
 int pbf_tape_destroy(pbf_tape* tape);
+/* Batched adjoint over `count` independent scenes, one handle each: the
+ * same tapes and gradients as pbf_forward / pbf_backward called scene by
+ * scene, but every scene's steps are enqueued (each on its handle's or its
+ * tape's stream) before any is waited for, so the scenes run side by side on
+ * the GPU, and each call synchronises once.  The handles (and the tapes) must
+ * be distinct; the tapes of one backward batch must have the same steps and
+ * checkpoint interval.  Arrays are indexed by scene: tapes[count] (out, all
+ * NULL on failure), d_pos_bar / d_vel_bar[count] (device pointers),
+ * d_pos0_bar / d_vel0_bar[count] (the arrays or their entries may be NULL)
+ * and xsph_c_bar (host float[count], may be NULL). */
+int pbf_forward_batch(pbf_sim* const* sims, int count, int steps, int checkpoint_every, pbf_tape** tapes);
+int pbf_backward_batch(pbf_tape* const* tapes, int count, const float4* const* d_pos_bar,
+                       const float4* const* d_vel_bar, float4* const* d_pos0_bar, float4* const* d_vel0_bar,
+                       float* xsph_c_bar);
 /* SPH density of the handle's state on res^3 cell centres of its grid box:
- * rho(g) = sum_i m W_poly6(|g - p_i|), into device float[res^3]. */
+ * rho(g) = sum_i m W_poly6(|g - p_i|), into device float[res^3].  Each
+ * particle adds its terms with float atomics, so the last bits of rho (and
+ * of the loss and gradient below) can differ from run to run. */
 int pbf_density_grid(pbf_sim* sim, int res, float* d_grid);
 /* loss = mean over the res^3 points of (rho(g) - target(g))^2 (target:
  * device float[res^3]); d_pos_bar (device float4[N], may be NULL) receives
