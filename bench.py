@@ -1059,11 +1059,16 @@ def main(argv=None):
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--loop-steps", type=int, default=0,
                     help="steps of the looped baseline (c4); 0 = the timed steps, the same window as the ensemble")
+    ap.add_argument("--scenes", type=int, default=0,
+                    help="number of scenes of c4 / c5 (0: the configuration's; fewer make small profiling runs)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world, rank, local = dist_setup()
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.scenes > 0 and "scenes" in cfg and args.scenes != cfg["scenes"]:
+        cfg["scenes"] = args.scenes
+        cfg["workload"] += " [run with %d scenes]" % args.scenes
     if args.impl == "reference":
         if cfg.get("adjoint"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}))
