@@ -389,7 +389,7 @@ def read_traffic(cfg, args):
     {"step": absolute step index, "phases": {phase: (DRAM bytes, warp
     instructions)}}, or None for other workloads."""
     tfile = os.path.join(ROOT, "profiles", "c2_dram_traffic.txt")
-    if cfg is not CONFIGS["c2"] or not os.path.exists(tfile):
+    if args.config != "c2" or not os.path.exists(tfile):
         return None
     step, phases = None, {}
     for ln in open(tfile):
@@ -1065,9 +1065,9 @@ def main(argv=None):
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world, rank, local = dist_setup()
-    cfg = dict(CONFIGS[args.config])
+    cfg = CONFIGS[args.config]
     if args.scenes > 0 and "scenes" in cfg and args.scenes != cfg["scenes"]:
-        cfg["scenes"] = args.scenes
+        cfg = dict(cfg, scenes=args.scenes)
         cfg["workload"] += " [run with %d scenes]" % args.scenes
     if args.impl == "reference":
         if cfg.get("adjoint"):

@@ -95,3 +95,14 @@ def test_oracle_scene_generation_matches_library(lib, orc, config):
     assert bytes(p_lib) == bytes(p_orc)
     assert C.sizeof(p_lib) == C.sizeof(p_orc)
     assert pos_lib.tobytes() == pos_orc.tobytes()
+
+
+def test_committed_step_profile_feeds_the_c2_line():
+    """The C2 line's DRAM traffic and issue roofline come from the committed
+    ncu figures of one step of its window (profiles/c2_dram_traffic.txt)."""
+    cap = bench.read_traffic(bench.CONFIGS["c2"], bench.argparse.Namespace(config="c2", steps=20, warmup=5))
+    assert cap is not None and 5 <= cap["step"] < 25
+    for phase in ("lists_1", "lambda_1", "delta_1", "lambda_2", "delta_2", "commit"):
+        dram, inst = cap["phases"][phase]
+        assert dram > 0 and inst > 0
+    assert bench.read_traffic(bench.CONFIGS["c3"], bench.argparse.Namespace(config="c3", steps=30, warmup=20)) is None
