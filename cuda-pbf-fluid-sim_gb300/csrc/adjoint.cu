@@ -689,6 +689,7 @@ struct pbf_tape {
     cudaStream_t stream = nullptr;
     // replay engine (the fused step's buffers)
     float4 *pos = nullptr, *vel = nullptr;
+    float4* xl = nullptr;  // the lambda pass's (x, y, z, lambda), read by the delta pass
     uint32_t* keys = nullptr;
     sim::DeviceParams* dp = nullptr;
     uint32_t* err = nullptr;
@@ -745,7 +746,7 @@ struct pbf_tape {
         b.key_s = r.key_s;
         b.perm = r.perm;
         b.pred_a = r.x[0];
-        b.pred_b = r.x[0];
+        b.pred_b = xl;
         b.pos_s = r.ps;
         b.vel_s = r.vf;
         b.lam_s = r.lam.empty() ? nullptr : r.lam[0];
@@ -770,10 +771,8 @@ struct pbf_tape {
         }
         for (int it = 0; it < iters; ++it) {
             FusedBufs bi = b;
-            float4* cur = r.x[it];
-            float4* nxt = r.x[it + 1];
-            bi.pred_a = (it % 2 == 0) ? cur : nxt;
-            bi.pred_b = (it % 2 == 0) ? nxt : cur;
+            bi.pred_a = r.x[it];
+            bi.pred_next = r.x[it + 1];
             bi.lam_s = r.lam[it];
             bi.delta_sum = r.D[it];
             bi.lambda_acc = r.A[it];
@@ -781,7 +780,7 @@ struct pbf_tape {
             if ((e = fused_solve_phase(bi, sh, it, 1, stream)) != cudaSuccess) return e;
         }
         FusedBufs bc = b;
-        bc.pred_a = bc.pred_b = r.x[std::max(iters, 0)];
+        bc.pred_a = r.x[std::max(iters, 0)];
         return fused_commit(bc, sh, stream);
     }
 
@@ -849,7 +848,7 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
         }
     }
     bool ok = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) == cudaSuccess && t->alloc(&t->pos, N) &&
-              t->alloc(&t->vel, N) && t->alloc(&t->keys, N) && t->alloc(&t->dp, 1) && t->alloc(&t->err, 1) &&
+              t->alloc(&t->vel, N) && t->alloc(&t->xl, N) && t->alloc(&t->keys, N) && t->alloc(&t->dp, 1) && t->alloc(&t->err, 1) &&
               t->alloc(reinterpret_cast<unsigned char**>(&t->sortTemp), t->sortBytes) && t->alloc(&t->pbar, N) &&
               t->alloc(&t->vbar, N) && t->alloc(&t->xfbar, N) && t->alloc(&t->vxbar, N) && t->alloc(&t->vfbar, N) &&
               t->alloc(&t->xbA, N) && t->alloc(&t->xbB, N) && t->alloc(&t->pbar_s, N) && t->alloc(&t->lambar, N) &&

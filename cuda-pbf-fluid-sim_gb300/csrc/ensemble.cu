@@ -119,7 +119,7 @@ struct pbf_ensemble {
         if (own) cudaStreamDestroy(own);
     }
 
-    float4* final_pred() const { return (passes % 2 == 0) ? pred_a : pred_b; }
+    float4* final_pred() const { return pred_a; }
 
     pbf::MultiBufs bufs() const {
         pbf::MultiBufs m{};

@@ -259,61 +259,41 @@ __device__ __forceinline__ RowSource row_source(const uint32_t* __restrict__ key
 }
 
 // Plans the CTA's tile and, when it is staged and its scene has lists, starts
-// copying the staged position rows into shared memory (sp[base[r] + i] =
-// pos[start[r] + i]): thread 0 issues one TMA bulk copy per row, completing on
-// the plan's barrier, while the other threads go on with their own loads.
-// Returns whether the tile is staged.  CTA-uniform; every thread calls it,
-// and every thread then calls stage_finish before reading the stage.  With
-// kBulk false nothing is issued and stage_rows fills the stage instead.
-template <class Sh, bool kBulk, class Scenes>
+// copying the staged rows into shared memory (sp[base[r] + i] = src[start[r]
+// + i]; src: positions, or the lambda pass's (x, y, z, lambda) for the delta
+// pass): thread 0 issues one TMA bulk copy per row, completing on the plan's
+// barrier, while the other threads go on with their own loads.  Returns
+// whether the tile is staged.  CTA-uniform; every thread calls it, and every
+// thread then calls stage_finish before reading the stage.
+template <class Sh, class Scenes>
 __device__ __forceinline__ bool plan_and_issue(TilePlan& P, const uint32_t* __restrict__ key_s,
                                                const uint32_t* __restrict__ lb, const Scenes& S,
                                                const ListBufs& lbuf, uint32_t t0, uint32_t N,
-                                               const float4* __restrict__ pos, float4* sp) {
+                                               const float4* __restrict__ src, float4* sp) {
     if (lbuf.cap == 0) return false;
     if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N);
-    if (kBulk && threadIdx.x == 0) mbar_init(&P.bar, 1);
+    if (threadIdx.x == 0) mbar_init(&P.bar, 1);
     __syncthreads();
     const bool staged = P.staged && P.lists && lbuf.staging;
-    if (kBulk && staged && threadIdx.x == 0) {
+    if (staged && threadIdx.x == 0) {
         // rows are float4 ranges: 16-byte aligned, sizes multiples of 16
         mbar_arrive_expect_tx(&P.bar, P.total * uint32_t(sizeof(float4)));
         for (int r = 0; r < P.nrows; ++r)
-            if (P.len[r]) bulk_copy_g2s(sp + P.base[r], pos + P.start[r], P.len[r] * uint32_t(sizeof(float4)), &P.bar);
+            if (P.len[r]) bulk_copy_g2s(sp + P.base[r], src + P.start[r], P.len[r] * uint32_t(sizeof(float4)), &P.bar);
     }
     return staged;
 }
 
-// Waits (bounded) for the staged rows, then fills in the rest of the stage:
-// w = lam[k] when lam is given; with vel given, w = vel[k].x and sv[i] =
-// (vel[k].y, vel[k].z).  A wait that gives up sets kErrStageTimeoutBit and
-// waits once more (also bounded) so that no copy is still landing when the
-// tile moves on; if that wait gives up too, in any thread, the stage is not
-// used: the function returns false and the tile's warps walk the stencil
-// from global memory instead.  CTA-uniform; every thread calls it.
-// The delta pass stages (x, y, z, lambda): a bulk copy of the positions
-// would need a second pass over the stage for lambda once it has landed, and
-// that measured slower than loading both in one pass, as here (sp[base[r] +
-// i] = (pos[k].xyz, lam[k]), k = start[r] + i), followed by a barrier.
+// Waits (bounded) for the staged rows, then, with vel given, fills in the
+// rest of the stage: w = vel[k].x and sv[i] = (vel[k].y, vel[k].z).  A wait
+// that gives up sets kErrStageTimeoutBit and waits once more (also bounded)
+// so that no copy is still landing when the tile moves on; if that wait gives
+// up too, in any thread, the stage is not used: the function returns false
+// and the tile's warps walk the stencil from global memory instead.
+// CTA-uniform; every thread calls it.
 template <class Sh>
-__device__ __forceinline__ void stage_rows(const TilePlan& P, bool staged, const float4* __restrict__ pos,
-                                           const float* __restrict__ lam, float4* sp) {
-    if (!staged) return;
-    for (int r = 0; r < P.nrows; ++r) {
-        const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
-        for (uint32_t i = threadIdx.x; i < len; i += Sh::kTile) {
-            float4 x = __ldg(pos + st + i);
-            x.w = __ldg(lam + st + i);
-            sp[bs + i] = x;
-        }
-    }
-    __syncthreads();
-}
-
-template <class Sh>
-__device__ __forceinline__ bool stage_finish(TilePlan& P, bool staged, const float* __restrict__ lam,
-                                             const float4* __restrict__ vel, float4* sp, float2* sv,
-                                             uint32_t* err) {
+__device__ __forceinline__ bool stage_finish(TilePlan& P, bool staged, const float4* __restrict__ vel, float4* sp,
+                                             float2* sv, uint32_t* err) {
     if (!staged) return true;
     bool landed = mbar_wait_bounded(&P.bar, 0u, kSpinLimit);
     if (!landed) {
@@ -321,17 +301,13 @@ __device__ __forceinline__ bool stage_finish(TilePlan& P, bool staged, const flo
         landed = mbar_wait_bounded(&P.bar, 0u, kSpinLimit);
     }
     if (__syncthreads_or(!landed)) return false;
-    if (!lam && !vel) return true;
+    if (!vel) return true;
     for (int r = 0; r < P.nrows; ++r) {
         const uint32_t st = P.start[r], bs = P.base[r], len = P.len[r];
         for (uint32_t i = threadIdx.x; i < len; i += Sh::kTile) {
-            float* w = reinterpret_cast<float*>(sp + bs + i) + 3;
-            if (lam) *w = __ldg(lam + st + i);
-            if (vel) {
-                const float4 v = __ldg(vel + st + i);
-                *w = v.x;
-                sv[bs + i] = make_float2(v.y, v.z);
-            }
+            const float4 v = __ldg(vel + st + i);
+            reinterpret_cast<float*>(sp + bs + i)[3] = v.x;
+            sv[bs + i] = make_float2(v.y, v.z);
         }
     }
     __syncthreads();
@@ -700,8 +676,8 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
     __shared__ uint32_t s_longest, s_over;
     float4* sp = smem;
     const uint32_t t0 = blockIdx.x * Sh::kTile;
-    const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
-    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
+    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, sp, nullptr, err);
     if (!staged || !stageOk) {  // CTA-uniform
         build_lists_warp<Scenes, Sh>(t0 + (threadIdx.x & ~31u), pred, key_s, lb, S, N, lbuf, list, count, stats);
         return;
@@ -797,12 +773,16 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
     }
 }
 
-// lambda of iteration `it` for every slot whose scene runs that iteration.
+// lambda of iteration `it` for every slot whose scene runs that iteration,
+// into lam[s] and, beside the slot's position, into xl[s] = (x, y, z,
+// lambda): the delta pass reads a neighbour's position and lambda with one
+// load, and stages its tile by bulk copies of xl.
 template <class Scenes, class Sh>
 __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, const float4* __restrict__ pred,
                                                   const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
                                                   Scenes S, uint32_t N, float* __restrict__ lam, ListBufs lbuf,
-                                                  uint32_t* __restrict__ err, float4* __restrict__ acc_out) {
+                                                  uint32_t* __restrict__ err, float4* __restrict__ acc_out,
+                                                  float4* __restrict__ xl) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -814,10 +794,10 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
     const float4 pi = pred[sc];
     const GlobalData g{pred, nullptr, nullptr};
-    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, nullptr, sp, nullptr, err);
+    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, sp, nullptr, err);
     uint32_t n;
     LambdaAcc a;
     if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
@@ -845,20 +825,26 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
         acc_out[2 * size_t(s)] = make_float4(a.density, a.sumGrad2, a.gx, a.gy);
         acc_out[2 * size_t(s) + 1] = make_float4(a.gz, float(a.contrib), __uint_as_float(a.last), 0.f);
     }
-    lam[s] = lambda_finalize(a, dp);
+    const float l = lambda_finalize(a, dp);
+    lam[s] = l;
+    xl[s] = make_float4(pi.x, pi.y, pi.z, l);
 }
 
-// delta of iteration `it`.  The scene's last iteration also applies the
-// post-solve boundary (e = 0) and computes v = (x - p)/dt; a scene past its
-// iterations carries its prediction through, and a scene without iterations
-// gets boundary and velocity in pass 0.
+// delta of iteration `it`: neighbours' positions and lambdas from the lambda
+// pass's xl, the slot's own prediction from pred (its w is kept) and lambda
+// from lam.  The scene's last iteration also applies the post-solve boundary
+// (e = 0) and computes v = (x - p)/dt; a scene past its iterations carries
+// its prediction through, and a scene without iterations gets boundary and
+// velocity in pass 0.  pred_out may be pred itself: a slot reads only its own
+// entry of pred, before writing it.
 template <class Scenes, class Sh, bool kFast>
-__global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, const float4* __restrict__ pred,
-                                                 const float* __restrict__ lam, const uint32_t* __restrict__ key_s,
-                                                 const uint32_t* __restrict__ lb, Scenes S, uint32_t N,
-                                                 float4* __restrict__ pred_out, const float4* __restrict__ pos_s,
-                                                 float4* __restrict__ vel_s, ListBufs lbuf,
-                                                 float4* __restrict__ dsum_out) {
+__global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, const float4* __restrict__ xl,
+                                                 const float4* pred, const float* __restrict__ lam,
+                                                 const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
+                                                 Scenes S, uint32_t N, float4* pred_out,
+                                                 const float4* __restrict__ pos_s, float4* __restrict__ vel_s,
+                                                 ListBufs lbuf, float4* __restrict__ dsum_out,
+                                                 uint32_t* __restrict__ err) {
     extern __shared__ float4 smem[];
     __shared__ TilePlan P;
     float4* sp = smem;
@@ -870,15 +856,15 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_issue<Sh, false>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
-    stage_rows<Sh>(P, staged, pred, lam, sp);
+    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, xl, sp);
     const float4 pi = pred[sc];
     const float lam_i = lam[sc];
     const float w_q = scorr_wq(dp);
-    const GlobalData g{pred, lam, nullptr};
+    const PackedData g{xl};
+    const bool stageOk = stage_finish<Sh>(P, staged, nullptr, sp, nullptr, err);
     uint32_t n;
     float3 d = make_float3(0.f, 0.f, 0.f);
-    if (warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+    if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i,
@@ -894,8 +880,9 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
             d = delta_of_sum<kFast>(sc, pi, lam_i, cx, cy, cz, dp, w_q, LbRows{lb + v.cellOffset},
                          [&](uint32_t k, uint32_t& j, float& lj) {
                              j = k;
-                             lj = __ldg(lam + k);
-                             return __ldg(pred + k);
+                             const float4 pk = __ldg(xl + k);
+                             lj = pk.w;
+                             return pk;
                          });
     } else {
         d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i, row_source(key_s, lb, v, sc), dp, w_q, g, q32);
@@ -957,8 +944,8 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
         float4* sp = smem;
         float2* sv = reinterpret_cast<float2*>(smem + Sh::kStageMax);
         const bool xs = s < N && dp.xsph_c > 0.f;  // every lane takes part in the warp-wide rounds
-        const bool staged = plan_and_issue<Sh, true>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
-        const bool stageOk = stage_finish<Sh>(P, staged, nullptr, vel_s, sp, sv, err);
+        const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+        const bool stageOk = stage_finish<Sh>(P, staged, vel_s, sp, sv, err);
         // Queue of the queued walks: the stage area, free in tiles that are
         // not staged.  In a staged tile a warp whose lists overflowed walks
         // the stencil without a queue.
@@ -1263,7 +1250,7 @@ cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, 
     if (sh.N == 0 || !lists_on(b, sh) || it < 0 || it >= sh.iters || it % sh.list_span != 0) return cudaErrorNotReady;
     const cudaError_t pe = fused_prepare_kernels();
     if (pe != cudaSuccess) return pe;
-    const float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
+    const float4* cur = b.pred_a;
     return with_tile_shape(sh.tile, [&](auto shape) {
         using Sh = decltype(shape);
         k_build_lists_tiled<OneScene, Sh><<<blocks_for(sh.N, Sh::kTile), Sh::kTile, Sh::kStageBytes, s>>>(
@@ -1277,9 +1264,12 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
     if (sh.N == 0 || it < 0 || it >= sh.iters) return cudaSuccess;
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
-    // iteration it reads buffer (it even ? a : b) and writes the other one
-    float4* cur = (it % 2 == 0) ? b.pred_a : b.pred_b;
-    float4* nxt = (it % 2 == 0) ? b.pred_b : b.pred_a;
+    // lambda reads the prediction in pred_a and writes (x, y, z, lambda) to
+    // pred_b; delta reads pred_b and writes the next prediction to pred_next
+    // (default: over pred_a)
+    float4* cur = b.pred_a;
+    float4* xl = b.pred_b;
+    float4* nxt = b.pred_next ? b.pred_next : b.pred_a;
     const OneScene sc = one_scene(b, sh, it);
     return with_tile_shape(sh.tile, [&](auto shape) {
         using Sh = decltype(shape);
@@ -1288,10 +1278,11 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
             const unsigned g = blocks_for(sh.N, Sh::kTile);
             if (which == 0)
                 k_lambda<OneScene, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
-                    it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh), b.err, b.lambda_acc);
+                    it, cur, b.key_s, b.lb, sc, sh.N, b.lam_s, list_bufs(b, sh), b.err, b.lambda_acc, xl);
             else
                 k_delta<OneScene, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
-                    it, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s, list_bufs(b, sh), b.delta_sum);
+                    it, xl, cur, b.lam_s, b.key_s, b.lb, sc, sh.N, nxt, b.pos_s, b.vel_s, list_bufs(b, sh),
+                    b.delta_sum, b.err);
             return cudaGetLastError();
         });
     });
@@ -1349,8 +1340,9 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
     if (m.N == 0) return cudaSuccess;
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
-    float4* cur = (it % 2 == 0) ? m.pred_a : m.pred_b;
-    float4* nxt = (it % 2 == 0) ? m.pred_b : m.pred_a;
+    // as fused_solve_phase: the prediction stays in pred_a, pred_b holds (x, y, z, lambda)
+    float4* cur = m.pred_a;
+    float4* xl = m.pred_b;
     const ManyScenes sc{m.scenes, m.sceneOfSlot};
     const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
     return with_tile_shape(m.tile, [&](auto shape) {
@@ -1360,10 +1352,10 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
             const unsigned g = blocks_for(m.N, Sh::kTile);
             if (which == 0)
                 k_lambda<ManyScenes, Sh><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(it, cur, m.key_s, m.lb, sc, m.N,
-                                                                                    m.lam_s, lb, m.err, nullptr);
+                                                                                    m.lam_s, lb, m.err, nullptr, xl);
             else
                 k_delta<ManyScenes, Sh, kFast><<<g, Sh::kTile, Sh::kSolveSmem, s>>>(
-                    it, cur, m.lam_s, m.key_s, m.lb, sc, m.N, nxt, m.pos_s, m.vel_s, lb, nullptr);
+                    it, xl, cur, m.lam_s, m.key_s, m.lb, sc, m.N, cur, m.pos_s, m.vel_s, lb, nullptr, m.err);
             return cudaGetLastError();
         });
     });

@@ -4,7 +4,10 @@
 //   pos, vel        float4[N]   committed state, original particle order
 //   keys            u32[N]      cell key of each particle's prediction (id order)
 //   key_s, perm     u32[N]      sorted keys and sorted->original ids
-//   pred_a, pred_b  float4[N]   predicted positions in cell order (ping-pong)
+//   pred_a          float4[N]   predicted positions in cell order (each solver
+//                               iteration's delta pass updates them in place)
+//   pred_b          float4[N]   (x, y, z, lambda) of the current iteration in
+//                               cell order (lambda pass -> delta pass)
 //   pos_s, vel_s    float4[N]   step-start positions / velocities in cell order
 //   lam_s           f32[N]      lambda in cell order
 //   lb              u32[numCells+1]  dense lower-bound table
@@ -29,6 +32,9 @@ struct FusedBufs {
     uint32_t* perm;
     float4* pred_a;
     float4* pred_b;
+    // Optional (null: pred_a): where the delta passes write the next
+    // prediction (the adjoint's replay keeps every iteration's).
+    float4* pred_next;
     // Optional (null: not written): the delta pass's neighbour sum per sorted
     // slot, before the displacement clamp (the adjoint's replay records it).
     float4* delta_sum;
@@ -130,9 +136,7 @@ cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, 
 // Number of list builds per step.
 int fused_list_builds(const FusedShape& sh);
 // Sorted buffer holding the solved prediction after fused_solve.
-inline float4* fused_final_pred(const FusedBufs& b, const FusedShape& sh) {
-    return (sh.iters % 2 == 0) ? b.pred_a : b.pred_b;
-}
+inline float4* fused_final_pred(const FusedBufs& b, const FusedShape&) { return b.pred_a; }
 
 // ------------------------------------------------------------ many scenes
 // One scene of a batch: its parameters, its first cell in the batch's global

@@ -480,6 +480,13 @@ struct GlobalData {
     __device__ __forceinline__ float l(uint32_t k, const float4&) const { return __ldg(lam + k); }
     __device__ __forceinline__ float4 v(uint32_t k) const { return __ldg(vel + k); }
 };
+// The lambda pass's (x, y, z, lambda) per sorted slot: the delta pass reads a
+// candidate's position and lambda with one load.
+struct PackedData {
+    const float4* __restrict__ xl;
+    __device__ __forceinline__ float4 p(uint32_t k) const { return __ldg(xl + k); }
+    __device__ __forceinline__ float l(uint32_t, const float4& pj) const { return pj.w; }
+};
 // Staged tile in shared memory: p_[k] = (x, y, z, w) with w = lambda (delta
 // passes) or the x velocity (XSPH, whose y and z velocities are in v_[k]).
 struct StagedData {

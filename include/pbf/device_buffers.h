@@ -5,9 +5,12 @@
 // cell-ordered arrays of the fused GB300 step.  Field meanings:
 //   d_pos, d_vel        committed state in ORIGINAL particle order (as the
 //                       reference's d_pos / d_vel)
-//   d_pos_pred          predicted positions in CELL order (sorted slots)
-//   d_pred_alt          second prediction buffer (Jacobi ping-pong; takes
-//                       the role of the reference's d_delta)
+//   d_pos_pred          predicted positions in CELL order (sorted slots);
+//                       each solver iteration's delta pass updates them
+//   d_pred_alt          (x, y, z, lambda) of the current iteration in cell
+//                       order: the lambda pass writes it, the delta pass
+//                       reads its neighbours from it (takes the role of the
+//                       reference's d_delta)
 //   d_pos_sorted        step-start positions in cell order
 //   d_vel_sorted        velocities in cell order (velocity phase output)
 //   d_lambda            lambda in cell order
@@ -19,9 +22,10 @@
 // against the reference's sim/device_buffers.cuh reads d_pos_pred and
 // d_lambda by particle id; here they are indexed by sorted slot s, whose
 // particle is d_indices_sorted[s].  d_delta, d_pos_curr and d_pos_next do not
-// exist: the Jacobi update ping-pongs between d_pos_pred and d_pred_alt
-// (SolvedPrediction below gives the last one) and the commit writes d_pos /
-// d_vel in place.  tests/cpp/plugin_path.cu is a worked example.
+// exist: the Jacobi update reads the iteration's positions from d_pred_alt
+// and writes the next ones over d_pos_pred (SolvedPrediction below gives the
+// buffer the Post phase reads), and the commit writes d_pos / d_vel in place.
+// tests/cpp/plugin_path.cu is a worked example.
 #pragma once
 
 #include <cstddef>
@@ -94,11 +98,9 @@ struct GridBuffers {
 };
 
 // The prediction the last solver iteration wrote (cell order), i.e. the
-// input of the Post phase: iteration `it` reads d_pos_pred when it is even
-// and writes d_pred_alt, and the other way round when it is odd.
-inline float4* SolvedPrediction(const DeviceBuffers& b, int solverIters) {
-    return (solverIters % 2 == 0) ? b.d_pos_pred : b.d_pred_alt;
-}
+// input of the Post phase: d_pos_pred for every iteration count.  (The
+// argument is kept so that callers need not change with the buffer scheme.)
+inline float4* SolvedPrediction(const DeviceBuffers& b, int /*solverIters*/) { return b.d_pos_pred; }
 
 class KernelDispatcher;
 
