@@ -726,15 +726,27 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
             ++cnt;
             if ((cnt & 7u) == 0u && cnt <= room) out[size_t((cnt >> 3) - 1u) * kListGroup] = make_uint4(w0, w1, w2, w3);
         };
-        for (int r = 0; r < nrows; ++r) {
+        // Slot range of stencil row r from the lower-bound table ([0, 0) for a
+        // row outside the grid).  Row r + 1's range is loaded before row r is
+        // walked, so its latency hides behind that walk.
+        auto row_range = [&](int r, uint32_t& rb, uint32_t& re) {
             const int z = cz + r / side - reach;
             const int y = cy + r % side - reach;
-            if (z < 0 || z >= dim.z || y < 0 || y >= dim.y) continue;
+            rb = re = 0u;
+            if (z < 0 || z >= dim.z || y < 0 || y >= dim.y) return;
             const uint32_t row = uint32_t((z * dim.y + y) * dim.x);
+            rb = __ldg(slb + row + uint32_t(x0));
+            re = __ldg(slb + row + uint32_t(x1) + 1u);
+        };
+        uint32_t nb, ne;
+        row_range(0, nb, ne);
+        for (int r = 0; r < nrows; ++r) {
+            const uint32_t rb = nb, re = ne;
+            if (r + 1 < nrows) row_range(r + 1, nb, ne);
             // the row lies inside the tile's staged range for offset r; the
             // clamp keeps every stage read in bounds regardless
-            const uint32_t b = max(__ldg(slb + row + uint32_t(x0)), P.start[r]);
-            const uint32_t e = min(__ldg(slb + row + uint32_t(x1) + 1u), P.start[r] + P.len[r]);
+            const uint32_t b = max(rb, P.start[r]);
+            const uint32_t e = min(re, P.start[r] + P.len[r]);
             const uint32_t shift = P.base[r] - P.start[r];  // stage index of slot k: k + shift
             shift_of_row = shift;
             // two candidates per round: both loads and tests in flight, then
