@@ -24,8 +24,8 @@ namespace pbf {
 
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 15;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 3840 keys per tile
+constexpr int kSortItems = 30;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 7680 keys per tile
 constexpr int kSortMaxPasses = 4;
 
 struct SortInfo {

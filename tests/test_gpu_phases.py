@@ -50,7 +50,8 @@ def scenes(lib, orc):
 # ----------------------------------------------------------------- sort
 SORT_CASES = [
     (1, "random"), (2, "random"), (31, "dup"), (2047, "random"), (2048, "dup"), (2049, "random"),
-    (3839, "random"), (3840, "dup"), (3841, "random"),
+    (3839, "random"), (3840, "dup"), (3841, "random"), (7679, "random"), (7680, "dup"), (7681, "random"),
+    (15_361, "random"),
     (100_000, "random"), (100_000, "dup"), (100_000, "equal"), (100_000, "sorted"), (100_000, "reverse"),
     (1 << 20, "cells"), (777_777, "random"),
 ]
