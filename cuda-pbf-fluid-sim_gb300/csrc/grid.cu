@@ -123,9 +123,6 @@ __global__ void k_lb_to_ranges(uint32_t* __restrict__ start, uint32_t* __restric
 }
 
 // ------------------------------------------------------------ compaction
-constexpr int kCompactThreads = 256;
-constexpr int kCompactItems = 8;
-constexpr int kCompactTile = kCompactThreads * kCompactItems;  // 2048 slots
 
 // Values of the compaction's count word besides a count (<= N < 2^30).
 constexpr uint32_t kCountPending = 0xFEFEFEFEu;  // a byte-wise memset value

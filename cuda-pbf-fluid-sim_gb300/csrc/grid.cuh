@@ -27,6 +27,12 @@ cudaError_t launch_cell_lb(uint32_t* lb, const uint32_t* keys_sorted, uint32_t N
 cudaError_t launch_lb_to_ranges(uint32_t* start, uint32_t* end, const uint32_t* lb, uint32_t numCells,
                                 cudaStream_t s);
 
+// Compaction tiles: kCompactThreads threads, kCompactItems sorted keys each
+// (one look-back status word per tile in the scratch).
+constexpr int kCompactThreads = 256;
+constexpr int kCompactItems = 16;
+constexpr int kCompactTile = kCompactThreads * kCompactItems;  // 4096 slots
+
 // Compact table (sim/cell_compact.cu): unique keys, segment offsets,
 // terminator and count, in one pass with decoupled look-back.  seg (may be
 // null) receives the segment index of every sorted slot.

@@ -1,7 +1,7 @@
 // noalloc.cu - cell-table compaction that allocates no device memory.
 //
 // pbf_launch_cell_ranges_compact needs a few KB of scratch (a tile counter
-// and one look-back status word per 2048 sorted keys), which its caller
+// and one look-back status word per tile of sorted keys), which its caller
 // allocates and passes in.  Some callers cannot do that while they run: a
 // host application's frame loop in which cudaMalloc / cudaFree would
 // synchronize the device and stall the frame, or a plugin host that budgets
@@ -26,9 +26,10 @@
 
 namespace {
 
-// 16,777,216 keys: 256 B header + one 4-byte status word per 2048-key tile.
+// 16,777,216 keys: 256 B header + one 4-byte status word per compaction tile.
 constexpr uint32_t kNoAllocMaxKeys = 1u << 24;
-constexpr size_t kNoAllocScratchBytes = 256 + ((size_t((kNoAllocMaxKeys + 2047u) / 2048u) * 4u + 255u) & ~size_t(255));
+constexpr size_t kNoAllocTiles = (size_t(kNoAllocMaxKeys) + pbf::kCompactTile - 1) / pbf::kCompactTile;
+constexpr size_t kNoAllocScratchBytes = 256 + ((kNoAllocTiles * 4u + 255u) & ~size_t(255));
 
 static __device__ __align__(256) unsigned char g_compact_scratch[kNoAllocScratchBytes];
 

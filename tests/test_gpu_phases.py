@@ -167,7 +167,7 @@ def test_hash_keys_and_tables_bit_exact(gpu, lib, orc, scenes, scene):
     np.testing.assert_array_equal(H(off).view(np.uint32)[: m + 1], ooff[: m + 1])
 
 
-@pytest.mark.parametrize("n", [0, 1, 2, 33, 2047, 2048, 2049, 70_001])
+@pytest.mark.parametrize("n", [0, 1, 2, 33, 2047, 2048, 2049, 4095, 4096, 4097, 70_001])
 def test_compact_and_dense_ragged(gpu, lib, orc, n):
     torch = gpu
     rng = np.random.default_rng(n + 11)
