@@ -98,6 +98,7 @@ struct pbf_ensemble {
     float* lam = nullptr;
     uint32_t *keys = nullptr, *key_s = nullptr, *perm = nullptr, *lb = nullptr, *sceneOfId = nullptr,
              *sceneOfSlot = nullptr, *err = nullptr, *nbrList = nullptr, *nbrCount = nullptr, *nbrStats = nullptr;
+    uint4* tilePlans = nullptr;  // the list build's tile plans (fused_tile_plan_bytes)
     uint32_t nbrCap = 0;
     int tile = 0;  // tile shape of the list passes
     bool fast = false;  // arithmetic of the delta pass (PBF_MATH_FAST)
@@ -114,7 +115,8 @@ struct pbf_ensemble {
         if (graph) cudaGraphDestroy(graph);
         for (void* p : {(void*)pos, (void*)vel, (void*)pred_a, (void*)pred_b, (void*)pos_s, (void*)vel_s, (void*)lam,
                         (void*)keys, (void*)key_s, (void*)perm, (void*)lb, (void*)sceneOfId, (void*)sceneOfSlot,
-                        (void*)err, (void*)scenes, sortTemp, (void*)nbrList, (void*)nbrCount, (void*)nbrStats})
+                        (void*)err, (void*)scenes, sortTemp, (void*)nbrList, (void*)nbrCount, (void*)nbrStats,
+                        (void*)tilePlans})
             if (p) cudaFree(p);
         if (own) cudaStreamDestroy(own);
     }
@@ -137,6 +139,7 @@ struct pbf_ensemble {
         m.perm = perm;
         m.lb = lb;
         m.nbr_list = nbrList;
+        m.tile_plans = tilePlans;
         m.nbr_count = nbrCount;
         m.nbr_stats = nbrStats;
         m.nbr_cap = nbrCap;
@@ -265,7 +268,8 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
     if (ok) {  // neighbour lists: optional (without them every scene walks the stencil)
         const uint32_t cap = sim::Simulator::kDefaultListCapacity;
         // whole groups of 32 slots: staged tiles interleave the lists of a group
-        if (dalloc(&e->nbrList, size_t((uint64_t(N) + 31u) & ~uint64_t(31)) * cap) && dalloc(&e->nbrCount, N)) {
+        if (dalloc(&e->nbrList, size_t((uint64_t(N) + 31u) & ~uint64_t(31)) * cap) && dalloc(&e->nbrCount, N) &&
+            dalloc(&e->tilePlans, pbf::fused_tile_plan_bytes(N) / sizeof(uint4))) {
             e->nbrCap = cap;
         } else {
             cudaGetLastError();

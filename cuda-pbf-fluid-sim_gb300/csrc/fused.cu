@@ -91,6 +91,10 @@ struct ListBufs {
     const uint32_t* __restrict__ count;
     uint32_t cap;  // 0: no lists
     int staging;   // 0: no tile is staged (all lists hold 32-bit slots)
+    // The step's tile plans (kPlanStride uint4 per tile, see store_plan):
+    // the list build writes them, the passes after it load them instead of
+    // planning again.  Null: every kernel plans its tiles itself.
+    uint4* plans;
 };
 
 // Whether slot s's scene has lists this pass (the builder decided the same).
@@ -221,12 +225,39 @@ __device__ WarpPlan plan_tile_warp(const uint32_t* __restrict__ key_s, const uin
     return w;
 }
 
-// The plan in shared memory for a CTA (written by warp 0).
+// A tile's plan in global memory: uint4 0 = (total, nrows, staged, 0),
+// uint4 1 + r = (start, base, len, 0) of row r.  The plan depends only on the
+// step's sorted keys, lower-bound table and tile shape, so every pass of a
+// step would compute the same one.
+constexpr int kPlanStride = kPlanRows + 1;
+
+// How plan_and_issue gets the CTA's plan.
+enum PlanMode { kPlanCompute = 0, kPlanStore = 1, kPlanLoad = 2 };
+
+// The plan in shared memory for a CTA (written by warp 0): computed, and with
+// kPlanStore also written to the step's plan array; or, with kPlanLoad,
+// loaded from there (row ranges, total, staged; the lists flag is this
+// pass's own).
 template <class Sh, class Scenes>
 __device__ void plan_tile(TilePlan& P, const uint32_t* __restrict__ key_s, const uint32_t* __restrict__ lb,
-                          const Scenes& S, const ListBufs& lbuf, uint32_t t0, uint32_t N) {
-    const WarpPlan w = plan_tile_warp<Sh>(key_s, lb, S, lbuf, t0, N);
+                          const Scenes& S, const ListBufs& lbuf, uint32_t t0, uint32_t N, PlanMode mode) {
     const int lane = int(threadIdx.x & 31u);
+    uint4* tp = lbuf.plans ? lbuf.plans + size_t(t0 / uint32_t(Sh::kTile)) * kPlanStride : nullptr;
+    if (mode == kPlanLoad && tp) {
+        const uint4 row = __ldg(tp + 1 + lane);
+        const uint4 head = __ldg(tp);
+        P.start[lane] = row.x;
+        P.base[lane] = row.y;
+        P.len[lane] = row.z;
+        if (lane == 0) {
+            P.total = head.x;
+            P.nrows = int(head.y);
+            P.staged = int(head.z);
+            P.lists = scene_lists(S.view(t0), lbuf) ? 1 : 0;
+        }
+        return;
+    }
+    const WarpPlan w = plan_tile_warp<Sh>(key_s, lb, S, lbuf, t0, N);
     P.start[lane] = w.start;
     P.base[lane] = w.base;
     P.len[lane] = w.len;
@@ -236,15 +267,26 @@ __device__ void plan_tile(TilePlan& P, const uint32_t* __restrict__ key_s, const
         P.staged = w.staged ? 1 : 0;
         P.lists = w.lists ? 1 : 0;
     }
+    if (mode == kPlanStore && tp) {
+        tp[1 + lane] = make_uint4(w.start, w.base, w.len, 0u);
+        if (lane == 0) tp[0] = make_uint4(w.total, uint32_t(w.nrows), w.staged ? 1u : 0u, 0u);
+    }
+}
+
+// The list length of slot sc, loaded before the tile's plan so that its
+// latency overlaps the plan's (0 without lists).
+__device__ __forceinline__ uint32_t list_count(const ListBufs& lbuf, uint32_t sc) {
+    return lbuf.cap ? __ldg(lbuf.count + sc) : 0u;
 }
 
 // Whether this warp walks its lists: every lane that walks has lists in its
-// scene and none of them overflowed.  Every lane must call it.
-__device__ __forceinline__ bool warp_lists_fit(const ListBufs& lbuf, bool active, bool laneLists, uint32_t sc,
+// scene and none of them overflowed (count: list_count of the lane's slot).
+// Every lane must call it.
+__device__ __forceinline__ bool warp_lists_fit(const ListBufs& lbuf, bool active, bool laneLists, uint32_t count,
                                                uint32_t& n) {
     n = 0;
     if (!__all_sync(0xFFFFFFFFu, !active || laneLists)) return false;
-    n = active ? lbuf.count[sc] : 0u;
+    n = active ? count : 0u;
     return !__any_sync(0xFFFFFFFFu, n > lbuf.cap);
 }
 
@@ -269,9 +311,10 @@ template <class Sh, class Scenes>
 __device__ __forceinline__ bool plan_and_issue(TilePlan& P, const uint32_t* __restrict__ key_s,
                                                const uint32_t* __restrict__ lb, const Scenes& S,
                                                const ListBufs& lbuf, uint32_t t0, uint32_t N,
-                                               const float4* __restrict__ src, float4* sp) {
+                                               const float4* __restrict__ src, float4* sp,
+                                               PlanMode mode = kPlanLoad) {
     if (lbuf.cap == 0) return false;
-    if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N);
+    if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N, mode);
     if (threadIdx.x == 0) mbar_init(&P.bar, 1);
     __syncthreads();
     const bool staged = P.staged && P.lists && lbuf.staging;
@@ -676,7 +719,8 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
     __shared__ uint32_t s_longest, s_over;
     float4* sp = smem;
     const uint32_t t0 = blockIdx.x * Sh::kTile;
-    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+    // the passes of this step load the plan this build stores
+    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp, kPlanStore);
     const bool stageOk = stage_finish<Sh>(P, staged, nullptr, sp, nullptr, err);
     if (!staged || !stageOk) {  // CTA-uniform
         build_lists_warp<Scenes, Sh>(t0 + (threadIdx.x & ~31u), pred, key_s, lb, S, N, lbuf, list, count, stats);
@@ -806,13 +850,15 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_lambda(int it, con
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
+    // the slot's own data first: its loads overlap the tile's plan
     const float4 pi = pred[sc];
+    const uint32_t cnt = list_count(lbuf, sc);
+    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
     const GlobalData g{pred, nullptr, nullptr};
     const bool stageOk = stage_finish<Sh>(P, staged, nullptr, sp, nullptr, err);
     uint32_t n;
     LambdaAcc a;
-    if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+    if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), cnt, n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             a = lambda_queued_acc<kQueue, Sh::kTile>(active, sc, pi,
@@ -868,15 +914,20 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinSolve) k_delta(int it, cons
     const SceneView v = S.view(sc);
     const sim::DeviceParams dp = *v.dp;  // in registers: the loops below never reload it
     const bool active = s < N && it < v.iters;  // every lane takes part in the warp-wide rounds
-    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, xl, sp);
+    // the slot's own data first: its loads overlap the tile's plan
     const float4 pi = pred[sc];
     const float lam_i = lam[sc];
+    // (the many-scene variant keeps the count load late: early, it spills)
+    constexpr bool kEarlyCount = std::is_same<Scenes, OneScene>::value;
+    const uint32_t cnt = kEarlyCount ? list_count(lbuf, sc) : 0u;
+    const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, xl, sp);
     const float w_q = scorr_wq(dp);
     const PackedData g{xl};
     const bool stageOk = stage_finish<Sh>(P, staged, nullptr, sp, nullptr, err);
     uint32_t n;
     float3 d = make_float3(0.f, 0.f, 0.f);
-    if (stageOk && warp_lists_fit(lbuf, active, scene_lists(v, lbuf), sc, n)) {
+    if (stageOk &&
+        warp_lists_fit(lbuf, active, scene_lists(v, lbuf), kEarlyCount ? cnt : list_count(lbuf, sc), n)) {
         const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
         if (staged)
             d = delta_queued_sum<kQueue, Sh::kTile, kFast>(active, sc, pi, lam_i,
@@ -956,6 +1007,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
         float4* sp = smem;
         float2* sv = reinterpret_cast<float2*>(smem + Sh::kStageMax);
         const bool xs = s < N && dp.xsph_c > 0.f;  // every lane takes part in the warp-wide rounds
+        const uint32_t cnt = list_count(lbuf, sc);
         const bool staged = plan_and_issue<Sh>(P, key_s, lb, S, lbuf, t0, N, pred, sp);
         const bool stageOk = stage_finish<Sh>(P, staged, vel_s, sp, sv, err);
         // Queue of the queued walks: the stage area, free in tiles that are
@@ -965,7 +1017,7 @@ __global__ void __launch_bounds__(Sh::kTile, Sh::kMinCommit) k_commit(const floa
         const GlobalData g{pred, nullptr, vel_s};
         uint32_t n;
         float4 vx = vv;
-        if (stageOk && warp_lists_fit(lbuf, xs, scene_lists(v, lbuf), sc, n)) {
+        if (stageOk && warp_lists_fit(lbuf, xs, scene_lists(v, lbuf), cnt, n)) {
             const uint32_t* base = lbuf.list + size_t(sc) * lbuf.cap;
             if (staged)
                 vx = xsph_list_inline(xs, x, vv,
@@ -1160,8 +1212,8 @@ int list_updates(const FusedShape& sh, int it) {
 }
 
 ListBufs list_bufs(const FusedBufs& b, const FusedShape& sh) {
-    if (!lists_on(b, sh)) return ListBufs{nullptr, nullptr, 0u, 0};
-    return ListBufs{b.nbr_list, b.nbr_count, b.nbr_cap, b.nbr_staging ? 1 : 0};
+    if (!lists_on(b, sh)) return ListBufs{nullptr, nullptr, 0u, 0, nullptr};
+    return ListBufs{b.nbr_list, b.nbr_count, b.nbr_cap, b.nbr_staging ? 1 : 0, b.tile_plans};
 }
 
 OneScene one_scene(const FusedBufs& b, const FusedShape& sh, int it) {
@@ -1227,6 +1279,17 @@ cudaError_t prepare_shape() {
 }  // namespace
 
 int fused_tile_shape_count() { return kTileShapeCount; }
+
+size_t fused_tile_plan_bytes(uint32_t capacity) {
+    int smallest = 1 << 30;
+    for (int id = 0; id < kTileShapeCount; ++id) {
+        int tile = 0, stage = 0;
+        fused_tile_shape_info(id, tile, stage);
+        smallest = std::min(smallest, tile);
+    }
+    const size_t tiles = (size_t(capacity) + size_t(smallest) - 1) / size_t(smallest) + 1;
+    return tiles * kPlanStride * sizeof(uint4);
+}
 
 bool fused_tile_shape_info(int id, int& tile, int& stage) {
     if (id < 0 || id >= kTileShapeCount) return false;
@@ -1338,7 +1401,7 @@ cudaError_t multi_build_lists(const MultiBufs& m, cudaStream_t s) {
     if (m.N == 0 || m.nbr_cap == 0) return cudaSuccess;
     const cudaError_t pe = fused_prepare_kernels();
     if (pe != cudaSuccess) return pe;
-    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1, m.tile_plans};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
         k_build_lists_tiled<ManyScenes, Sh><<<blocks_for(m.N, Sh::kTile), Sh::kTile, Sh::kStageBytes, s>>>(
@@ -1356,7 +1419,7 @@ cudaError_t multi_solve_phase(const MultiBufs& m, int it, int which, cudaStream_
     float4* cur = m.pred_a;
     float4* xl = m.pred_b;
     const ManyScenes sc{m.scenes, m.sceneOfSlot};
-    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1, m.tile_plans};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
         return with_math(m.fast, [&](auto fast) {
@@ -1377,7 +1440,7 @@ cudaError_t multi_commit(const MultiBufs& m, const float4* final_pred, cudaStrea
     if (m.N == 0) return cudaSuccess;
     cudaError_t e = fused_prepare_kernels();
     if (e != cudaSuccess) return e;
-    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1};
+    const ListBufs lb{m.nbr_list, m.nbr_count, m.nbr_cap, 1, m.tile_plans};
     return with_tile_shape(m.tile, [&](auto shape) {
         using Sh = decltype(shape);
         k_commit<ManyScenes, true, Sh><<<blocks_for(m.N, Sh::kTile), Sh::kTile, Sh::kCommitSmem, s>>>(

@@ -35,6 +35,10 @@ struct FusedBufs {
     // Optional (null: pred_a): where the delta passes write the next
     // prediction (the adjoint's replay keeps every iteration's).
     float4* pred_next;
+    // Optional (null: each list pass plans its tiles): fused_tile_plan_bytes
+    // of scratch where the list build stores the step's tile plans for the
+    // passes after it.
+    uint4* tile_plans;
     // Optional (null: not written): the delta pass's neighbour sum per sorted
     // slot, before the displacement clamp (the adjoint's replay records it).
     float4* delta_sum;
@@ -133,6 +137,9 @@ cudaError_t fused_solve_phase(const FusedBufs& b, const FusedShape& sh, int it, 
 // Builds the neighbour lists if iteration `it` starts a list span; returns
 // cudaErrorNotReady (and launches nothing) when it does not.
 cudaError_t fused_build_lists(const FusedBufs& b, const FusedShape& sh, int it, cudaStream_t s);
+// Bytes of FusedBufs::tile_plans for up to `capacity` particles (every tile
+// shape).
+size_t fused_tile_plan_bytes(uint32_t capacity);
 // Number of list builds per step.
 int fused_list_builds(const FusedShape& sh);
 // Sorted buffer holding the solved prediction after fused_solve.
@@ -160,6 +167,7 @@ struct MultiBufs {
     const uint32_t *key_s, *perm, *lb;
     uint32_t *nbr_list, *nbr_count, *nbr_stats;
     uint32_t nbr_cap;  // 0: no lists
+    uint4* tile_plans; // as FusedBufs::tile_plans
     uint32_t* err;     // device error word (kErr* bits)
     int tile;          // tile shape of the list passes
     bool fast;         // arithmetic of the delta pass (FusedShape::fast)

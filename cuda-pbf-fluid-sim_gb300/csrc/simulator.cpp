@@ -66,6 +66,7 @@ pbf::FusedBufs fused_bufs(DeviceBuffers& b, GridBuffers& g) {
     f.stats_out = b.d_stats;
     f.stats_partials = b.d_stats + 4;
     f.nbr_list = b.d_nbrList;
+    f.tile_plans = b.d_tilePlans;
     f.nbr_count = b.d_nbrCount;
     f.nbr_stats = b.d_nbrStats;
     f.nbr_cap = b.nbrListCap;
@@ -154,7 +155,8 @@ bool DeviceBuffers::allocateLists(uint32_t entries) {
     if (entries == 0 || capacity == 0) return true;
     // whole groups of 32 slots: staged tiles interleave the lists of a group
     const size_t n = size_t((capacity + 31u) & ~31u) * entries;
-    if (!dalloc(&d_nbrList, n) || !dalloc(&d_nbrCount, capacity) || !dalloc(&d_nbrStats, 2)) {
+    if (!dalloc(&d_nbrList, n) || !dalloc(&d_nbrCount, capacity) || !dalloc(&d_nbrStats, 2) ||
+        !dalloc(&d_tilePlans, pbf::fused_tile_plan_bytes(capacity) / sizeof(uint4))) {
         releaseLists();
         cudaGetLastError();
         return false;
@@ -166,6 +168,7 @@ bool DeviceBuffers::allocateLists(uint32_t entries) {
 
 void DeviceBuffers::releaseLists() {
     dfree(d_nbrList);
+    dfree(d_tilePlans);
     dfree(d_nbrCount);
     dfree(d_nbrStats);
     nbrListCap = 0;

@@ -53,6 +53,7 @@ struct DeviceBuffers {
     // Neighbour lists of the GB300 step (cell order, nbrListCap entries per
     // particle; nbrListCap = 0: no lists, every pass walks the stencil).
     uint32_t* d_nbrList = nullptr;
+    uint4* d_tilePlans = nullptr;  // the list build's tile plans, read by the passes after it (scratch)
     uint32_t* d_nbrCount = nullptr;
     uint32_t* d_nbrStats = nullptr;  // [0] longest list built, [1] overflowed lists
     uint32_t nbrListCap = 0;
