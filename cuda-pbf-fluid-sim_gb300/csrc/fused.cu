@@ -91,7 +91,7 @@ struct ListBufs {
     const uint32_t* __restrict__ count;
     uint32_t cap;  // 0: no lists
     int staging;   // 0: no tile is staged (all lists hold 32-bit slots)
-    // The step's tile plans (kPlanStride uint4 per tile, see store_plan):
+    // The step's tile plans (kPlanStride uint4 per tile, see plan_tile):
     // the list build writes them, the passes after it load them instead of
     // planning again.  Null: every kernel plans its tiles itself.
     uint4* plans;
