@@ -106,3 +106,14 @@ def test_committed_step_profile_feeds_the_c2_line():
         dram, inst = cap["phases"][phase]
         assert dram > 0 and inst > 0
     assert bench.read_traffic(bench.CONFIGS["c3"], bench.argparse.Namespace(config="c3", steps=30, warmup=20)) is None
+
+
+def test_dominant_kernel_counts_every_launch():
+    """The roofline's kernel is the one with the most time over all its
+    launches in a step, not the longest single launch."""
+    ph = {"predict_keys": 0.011, "sort": 0.075, "lists_1": 0.238, "lambda_1": 0.116, "delta_1": 0.177,
+          "lambda_2": 0.116, "delta_2": 0.182, "commit": 0.143}
+    dom, members, ms = bench.dominant_kernel(ph)
+    assert dom == "delta" and members == ["delta_1", "delta_2"] and abs(ms - 0.359) < 1e-9
+    dom, members, ms = bench.dominant_kernel({"lists_1": 0.3, "delta_1": 0.2, "commit": 0.1})
+    assert dom == "lists" and members == ["lists_1"]
