@@ -1163,13 +1163,37 @@ cudaError_t fused_sort(const FusedBufs& b, const FusedShape& sh, cudaStream_t s)
 }
 
 cudaError_t fused_gather_and_tables(const FusedBufs& b, const FusedShape& sh, cudaStream_t s) {
-    if (sh.N > 0) k_gather<<<blocks_for(sh.N, kBS), kBS, 0, s>>>(b.perm, b.pos, b.vel, b.dp, sh.N, b.pred_a, b.pos_s);
-    cudaError_t e = launch_cell_lb(b.lb, b.key_s, sh.N, sh.numCells, s);
-    if (e != cudaSuccess) return e;
-    if (sh.hashed) {
-        e = launch_compact(b.compact_temp, b.compact_bytes, b.uk, b.off, b.count, nullptr, b.key_s, sh.N, s, b.err);
-        if (e != cudaSuccess) return e;
+    // The gather, the lower-bound table and the compact table read only the
+    // sorted keys and permutation, and write disjoint buffers: with the fork
+    // resources they run side by side (each is a few small, latency-bound
+    // kernels), joined back on s.
+    const bool fork = b.fork_streams[0] && b.fork_streams[1] && b.fork_events[0] && b.fork_events[1] &&
+                      b.fork_events[2];
+    cudaStream_t s_lb = s, s_cp = s;
+    cudaError_t e;
+    if (fork) {
+        if ((e = cudaEventRecord(b.fork_events[0], s)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(b.fork_streams[0], b.fork_events[0], 0)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(b.fork_streams[1], b.fork_events[0], 0)) != cudaSuccess)
+            return e;
+        s_lb = b.fork_streams[0];
+        s_cp = b.fork_streams[1];
     }
+    if (sh.N > 0) k_gather<<<blocks_for(sh.N, kBS), kBS, 0, s>>>(b.perm, b.pos, b.vel, b.dp, sh.N, b.pred_a, b.pos_s);
+    e = launch_cell_lb(b.lb, b.key_s, sh.N, sh.numCells, s_lb);
+    if (e == cudaSuccess && sh.hashed)
+        e = launch_compact(b.compact_temp, b.compact_bytes, b.uk, b.off, b.count, nullptr, b.key_s, sh.N, s_cp, b.err);
+    if (fork) {
+        // join even after a failed launch, so that a capture stays well formed
+        const cudaError_t j = (cudaEventRecord(b.fork_events[1], s_lb) == cudaSuccess &&
+                               cudaEventRecord(b.fork_events[2], s_cp) == cudaSuccess &&
+                               cudaStreamWaitEvent(s, b.fork_events[1], 0) == cudaSuccess &&
+                               cudaStreamWaitEvent(s, b.fork_events[2], 0) == cudaSuccess)
+                                  ? cudaSuccess
+                                  : cudaErrorUnknown;
+        if (e == cudaSuccess) e = j;
+    }
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -39,6 +39,11 @@ struct FusedBufs {
     // of scratch where the list build stores the step's tile plans for the
     // passes after it.
     uint4* tile_plans;
+    // Optional (any null: one stream): side streams and events on which
+    // fused_gather_and_tables runs the lower-bound and compact tables beside
+    // the gather, joined back on its stream before it returns.
+    cudaStream_t fork_streams[2];
+    cudaEvent_t fork_events[3];
     // Optional (null: not written): the delta pass's neighbour sum per sorted
     // slot, before the displacement clamp (the adjoint's replay records it).
     float4* delta_sum;

@@ -67,6 +67,8 @@ pbf::FusedBufs fused_bufs(DeviceBuffers& b, GridBuffers& g) {
     f.stats_partials = b.d_stats + 4;
     f.nbr_list = b.d_nbrList;
     f.tile_plans = b.d_tilePlans;
+    for (int k = 0; k < 2; ++k) f.fork_streams[k] = b.forkStreams[k];
+    for (int k = 0; k < 3; ++k) f.fork_events[k] = b.forkEvents[k];
     f.nbr_count = b.d_nbrCount;
     f.nbr_stats = b.d_nbrStats;
     f.nbr_cap = b.nbrListCap;
@@ -289,6 +291,10 @@ bool Simulator::initialize(const SimParams& p, bool useHashedGrid) {
     if (nc == 0) return false;
     if (cudaStreamCreateWithFlags(&m_ownStream, cudaStreamNonBlocking) != cudaSuccess) return false;
     m_stream = m_ownStream;
+    for (cudaStream_t& fs : m_bufs.forkStreams)
+        if (cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking) != cudaSuccess) return false;
+    for (cudaEvent_t& fe : m_bufs.forkEvents)
+        if (cudaEventCreateWithFlags(&fe, cudaEventDisableTiming) != cudaSuccess) return false;
     uint32_t cap = std::max(p.maxParticles, p.numParticles);
     if (cap == 0) cap = 1;
     if (!m_bufs.allocate(cap)) return false;
@@ -320,6 +326,17 @@ void Simulator::shutdown() {
         m_ownStream = nullptr;
     }
     m_stream = nullptr;
+    for (cudaStream_t& fs : m_bufs.forkStreams)
+        if (fs) {
+            cudaStreamSynchronize(fs);
+            cudaStreamDestroy(fs);
+            fs = nullptr;
+        }
+    for (cudaEvent_t& fe : m_bufs.forkEvents)
+        if (fe) {
+            cudaEventDestroy(fe);
+            fe = nullptr;
+        }
     m_bufs.release();
     m_grid.release();
     m_paramsValid = false;

@@ -63,6 +63,12 @@ struct DeviceBuffers {
     // Arithmetic of the delta pass: 0 exact (bit-identical to the reference
     // kernels), 1 fast (within the 1e-5 bars; PBF_MATH_FAST).
     int mathMode = 0;
+    // Fork-join resources of the grid build: after the sort, the gather, the
+    // lower-bound table and the compact table each read only the sorted keys,
+    // so they run on the step's stream and these two side streams at once
+    // (joined back before the lists are built).  Null: one after another.
+    cudaStream_t forkStreams[2] = {nullptr, nullptr};
+    cudaEvent_t forkEvents[3] = {nullptr, nullptr, nullptr};
 
     bool allocate(uint32_t cap);
     // (Re)allocates the lists for `capacity` particles; entries is rounded up
