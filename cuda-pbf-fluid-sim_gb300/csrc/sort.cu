@@ -20,7 +20,8 @@ SortLayout layout_for(uint32_t N, int num_bits) {
     L.passes = (num_bits + 7) / 8;
     if (L.passes < 1) L.passes = 1;
     if (L.passes > kSortMaxPasses) L.passes = kSortMaxPasses;
-    L.tiles = (N + kSortTile - 1) / kSortTile;
+    const uint32_t tile = uint32_t(kSortThreads * sort_items_for(N));
+    L.tiles = (N + tile - 1) / tile;
     if (L.tiles == 0) L.tiles = 1;
     L.info_off = 0;
     L.status_off = align_up(sizeof(SortInfo));
@@ -115,6 +116,7 @@ __device__ __forceinline__ const uint32_t* pick_src_vals(const SortBufs& b, uint
     return id == 0u ? b.vals_in : (id == 1u ? b.vals_alt : b.vals_out);
 }
 
+template <int kSortItems>
 __global__ void __launch_bounds__(kSortThreads) k_sort_pass(SortBufs b, uint32_t N, int begin_bit, int end_bit,
                                                             int pass, int last_pass, SortInfo* info,
                                                             uint32_t* status, uint32_t* err) {
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(SortBufs b, uint32_t
     uint32_t* kout = dst == 2u ? b.keys_out : b.keys_alt;
     uint32_t* vout = dst == 2u ? b.vals_out : b.vals_alt;
 
-    const uint32_t base = tile * uint32_t(kSortTile) + uint32_t(warp) * (32u * kSortItems) + uint32_t(lane);
+    const uint32_t base = tile * uint32_t(kSortThreads * kSortItems) + uint32_t(warp) * (32u * kSortItems) + uint32_t(lane);
     uint32_t keys[kSortItems], vals[kSortItems], rank[kSortItems];
 #pragma unroll
     for (int j = 0; j < kSortItems; ++j) {
@@ -229,7 +231,8 @@ cudaError_t sort_pairs(void* d_temp, size_t temp_bytes, const uint32_t* keys_in,
     if (hb < 1u) hb = 1u;
     k_sort_hist<<<hb, 256, 0, s>>>(keys_in, N, 0, num_bits, L.passes, info);
     for (int p = 0; p < L.passes; ++p) {
-        k_sort_pass<<<L.tiles, kSortThreads, 0, s>>>(b, N, 0, num_bits, p, L.passes - 1, info,
+        const auto pass = sort_items_for(N) == kSortItemsLarge ? k_sort_pass<kSortItemsLarge> : k_sort_pass<kSortItemsSmall>;
+        pass<<<L.tiles, kSortThreads, 0, s>>>(b, N, 0, num_bits, p, L.passes - 1, info,
                                                      status + size_t(p) * L.tiles * 256u, err);
     }
     return cudaGetLastError();

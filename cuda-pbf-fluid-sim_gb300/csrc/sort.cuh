@@ -24,8 +24,13 @@ namespace pbf {
 
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 30;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 7680 keys per tile
+// Keys per thread of a pass: large sorts take 30 (7,680 per tile, so that a
+// 1M-key pass is one wave of 137 tiles with short look-back chains), small
+// ones 15 (more, shorter tiles: at 65,536 keys 18 tiles instead of 9).
+constexpr int kSortItemsSmall = 15;
+constexpr int kSortItemsLarge = 30;
+constexpr uint32_t kSortLargeFrom = 1u << 19;  // keys
+inline int sort_items_for(uint32_t N) { return N >= kSortLargeFrom ? kSortItemsLarge : kSortItemsSmall; }
 constexpr int kSortMaxPasses = 4;
 
 struct SortInfo {

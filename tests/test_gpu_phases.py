@@ -51,7 +51,7 @@ def scenes(lib, orc):
 SORT_CASES = [
     (1, "random"), (2, "random"), (31, "dup"), (2047, "random"), (2048, "dup"), (2049, "random"),
     (3839, "random"), (3840, "dup"), (3841, "random"), (7679, "random"), (7680, "dup"), (7681, "random"),
-    (15_361, "random"),
+    (15_361, "random"), (524_287, "random"), (524_288, "dup"), (614_401, "random"),
     (100_000, "random"), (100_000, "dup"), (100_000, "equal"), (100_000, "sorted"), (100_000, "reverse"),
     (1 << 20, "cells"), (777_777, "random"),
 ]
