@@ -750,6 +750,7 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
         const int x1 = min(cx + reach, dim.x - 1);
         const uint32_t* __restrict__ slb = lb + v.cellOffset;
         const float4 pi = pred[s];
+        const unsigned long long ix = pk2(pi.x, pi.x), iy = pk2(pi.y, pi.y), iz = pk2(pi.z, pi.z);
         // the interleaved 16-bit list: chunk c at out[c * kListGroup] (2 cap entries of room)
         uint4* out = reinterpret_cast<uint4*>(list16_base(list, cap, s));
         const uint32_t room = 2u * cap;
@@ -797,10 +798,13 @@ __global__ void __launch_bounds__(Sh::kTile) k_build_lists_tiled(const float4* _
             // the hits emitted in walk order
             uint32_t k = b;
             for (; k + 1u < e; k += 2u) {
-                float rx, ry, rz;
                 const float4 pa = sp[k + shift], pb = sp[k + 1u + shift];
-                const bool ha = k != s && !(dist2(pi, pa, rx, ry, rz) > R2);
-                const bool hb = k + 1u != s && !(dist2(pi, pb, rx, ry, rz) > R2);
+                // both candidates' r^2 at once (f32x2: each half is dist2's arithmetic)
+                const unsigned long long dx = sub2(ix, pk2(pa.x, pb.x)), dy = sub2(iy, pk2(pa.y, pb.y)),
+                                         dz = sub2(iz, pk2(pa.z, pb.z));
+                const float2 r2 = upk2(fma2(dz, dz, fma2(dx, dx, mul2(dy, dy))));
+                const bool ha = k != s && !(r2.x > R2);
+                const bool hb = k + 1u != s && !(r2.y > R2);
                 if (ha) emit(k);
                 if (hb) emit(k + 1u);
             }
