@@ -313,7 +313,9 @@ __device__ __forceinline__ bool plan_and_issue(TilePlan& P, const uint32_t* __re
                                                const ListBufs& lbuf, uint32_t t0, uint32_t N,
                                                const float4* __restrict__ src, float4* sp,
                                                PlanMode mode = kPlanLoad) {
-    if (lbuf.cap == 0) return false;
+    // no lists, or lists of 32-bit slots only (the adjoint's replay): no tile
+    // is staged, and no plan is needed
+    if (lbuf.cap == 0 || !lbuf.staging) return false;
     if (threadIdx.x < 32) plan_tile<Sh>(P, key_s, lb, S, lbuf, t0, N, mode);
     if (threadIdx.x == 0) mbar_init(&P.bar, 1);
     __syncthreads();
