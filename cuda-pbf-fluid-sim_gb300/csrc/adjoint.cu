@@ -880,7 +880,8 @@ int make_tape(const sim::SimParams& sp, uint32_t N, int steps, int every, bool x
         const sim::DeviceParams dp = sim::MakeDeviceParams(sp);
         ok = cudaMemcpy(t->dp, &dp, sizeof(dp), cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMemset(t->err, 0, sizeof(uint32_t)) == cudaSuccess &&
-             cudaMemset(t->listStats, 0, 2 * sizeof(uint32_t)) == cudaSuccess && fused_prepare_kernels() == cudaSuccess;
+             cudaMemset(t->listStats, 0, 2 * sizeof(uint32_t)) == cudaSuccess && fused_prepare_kernels() == cudaSuccess &&
+             cudaDeviceSynchronize() == cudaSuccess;  // the legacy-stream setup, before the tape's stream runs
     }
     if (!ok) {
         const cudaError_t e = cudaGetLastError();

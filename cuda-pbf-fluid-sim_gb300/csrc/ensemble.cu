@@ -285,7 +285,10 @@ int pbf_ensemble_create(const pbf_sim_params* params, uint32_t num_scenes, pbf_e
                  cudaSuccess &&
              cudaMemset(e->pos, 0, sizeof(float4) * std::max<uint32_t>(N, 1)) == cudaSuccess &&
              cudaMemset(e->vel, 0, sizeof(float4) * std::max<uint32_t>(N, 1)) == cudaSuccess &&
-             cudaMemset(e->err, 0, sizeof(uint32_t)) == cudaSuccess;
+             cudaMemset(e->err, 0, sizeof(uint32_t)) == cudaSuccess &&
+             // legacy-stream copies and clears, finished before the ensemble's
+             // non-blocking stream runs
+             cudaDeviceSynchronize() == cudaSuccess;
     }
     if (!ok) {
         const cudaError_t ce = cudaGetLastError();
@@ -438,7 +441,7 @@ int pbf_ensemble_autotune(pbf_ensemble* e, int steps, float* ms, int* chosen) {
     if (snap && !(restore() && cudaStreamSynchronize(e->stream) == cudaSuccess) && st == PBF_OK) st = PBF_ERR_CUDA;
     const int st2 = e->set_tile(st == PBF_OK ? best : before);
     if (st == PBF_OK) st = st2;
-    if (e->nbrStats) cudaMemset(e->nbrStats, 0, 2 * sizeof(uint32_t));
+    if (e->nbrStats) cudaMemsetAsync(e->nbrStats, 0, 2 * sizeof(uint32_t), e->stream);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (snap) cudaFree(snap);

@@ -148,7 +148,9 @@ bool DeviceBuffers::allocate(uint32_t cap) {
     cudaMemset(d_pos, 0, sizeof(float4) * cap);
     cudaMemset(d_vel, 0, sizeof(float4) * cap);
     cudaMemset(d_err, 0, sizeof(uint32_t));
-    return true;
+    // the clears run on the legacy stream, which the simulator's non-blocking
+    // streams do not wait for: finish them before any step is launched
+    return cudaDeviceSynchronize() == cudaSuccess;
 }
 
 bool DeviceBuffers::allocateLists(uint32_t entries) {
@@ -165,7 +167,7 @@ bool DeviceBuffers::allocateLists(uint32_t entries) {
     }
     cudaMemset(d_nbrStats, 0, 2 * sizeof(uint32_t));
     nbrListCap = entries;
-    return true;
+    return cudaDeviceSynchronize() == cudaSuccess;  // as in allocate
 }
 
 void DeviceBuffers::releaseLists() {
@@ -210,7 +212,7 @@ bool GridBuffers::allocate(uint32_t cap, uint32_t nCells) {
         return false;
     }
     cudaMemset(d_compactCount, 0, sizeof(uint32_t));
-    return true;
+    return cudaDeviceSynchronize() == cudaSuccess;  // as in DeviceBuffers::allocate
 }
 
 bool GridBuffers::ensureRangesMaterialised() {
@@ -373,8 +375,11 @@ bool Simulator::ensureCapacity(uint32_t n) {
     m_bufs.allocateLists(m_listCapacity);
     m_bufs.xsphEnabled = xs;
     m_grid.hashed = m_useHashedGrid;
-    cudaMemcpy(m_bufs.d_pos, pos.data(), sizeof(float4) * pos.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(m_bufs.d_vel, vel.data(), sizeof(float4) * vel.size(), cudaMemcpyHostToDevice);
+    // on the simulator's stream (non-blocking: the legacy stream's copies are
+    // not ordered before its launches); a pageable source is staged before
+    // the call returns
+    cudaMemcpyAsync(m_bufs.d_pos, pos.data(), sizeof(float4) * pos.size(), cudaMemcpyHostToDevice, m_stream);
+    cudaMemcpyAsync(m_bufs.d_vel, vel.data(), sizeof(float4) * vel.size(), cudaMemcpyHostToDevice, m_stream);
     m_paramsValid = false;
     m_graphDirty = true;
     return true;
@@ -523,7 +528,7 @@ bool Simulator::neighbourListStats(uint32_t& longest, uint32_t& overflowed, bool
     if (cudaMemcpy(v, m_bufs.d_nbrStats, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess) return false;
     longest = v[0];
     overflowed = v[1];
-    if (reset) cudaMemset(m_bufs.d_nbrStats, 0, sizeof(v));
+    if (reset) cudaMemsetAsync(m_bufs.d_nbrStats, 0, sizeof(v), m_stream);
     return true;
 }
 
@@ -618,11 +623,12 @@ void Simulator::uploadPositions(const std::vector<float4>& pos, const std::vecto
     const uint32_t n = uint32_t(pos.size());
     ensureCapacity(n);
     cudaStreamSynchronize(m_stream);
-    cudaMemcpy(m_bufs.d_pos, pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice);
+    // ordered on the simulator's stream before the next step (see ensureCapacity)
+    cudaMemcpyAsync(m_bufs.d_pos, pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, m_stream);
     if (vel)
-        cudaMemcpy(m_bufs.d_vel, vel->data(), sizeof(float4) * n, cudaMemcpyHostToDevice);
+        cudaMemcpyAsync(m_bufs.d_vel, vel->data(), sizeof(float4) * n, cudaMemcpyHostToDevice, m_stream);
     else
-        cudaMemset(m_bufs.d_vel, 0, sizeof(float4) * n);
+        cudaMemsetAsync(m_bufs.d_vel, 0, sizeof(float4) * n, m_stream);
     if (m_params.numParticles != n) m_graphDirty = true;
     m_params.numParticles = n;
 }
