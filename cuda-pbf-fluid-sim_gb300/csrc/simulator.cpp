@@ -629,6 +629,7 @@ void Simulator::uploadPositions(const std::vector<float4>& pos, const std::vecto
         cudaMemcpyAsync(m_bufs.d_vel, vel->data(), sizeof(float4) * n, cudaMemcpyHostToDevice, m_stream);
     else
         cudaMemsetAsync(m_bufs.d_vel, 0, sizeof(float4) * n, m_stream);
+    cudaStreamSynchronize(m_stream);  // blocking, as the reference's upload
     if (m_params.numParticles != n) m_graphDirty = true;
     m_params.numParticles = n;
 }
