@@ -59,7 +59,19 @@ __global__ void __launch_bounds__(256) k_sort_hist(const uint32_t* __restrict__ 
     const int t = threadIdx.x;
     for (int p = 0; p < passes; ++p) sh[p][t] = 0u;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + t; i < N; i += gridDim.x * blockDim.x) {
+    // eight keys per thread loaded before any is counted, so their load
+    // latencies overlap instead of following each other
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t i = blockIdx.x * blockDim.x + t;
+    for (; i < N && N - i > 7u * stride; i += 8u * stride) {
+        uint32_t k[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) k[u] = __ldg(keys + i + uint32_t(u) * stride);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][digit_of(k[u], begin_bit, end_bit, p)], 1u);
+    }
+    for (; i < N; i += stride) {
         const uint32_t k = keys[i];
         for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][digit_of(k, begin_bit, end_bit, p)], 1u);
     }
